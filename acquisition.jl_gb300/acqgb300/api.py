@@ -1,0 +1,420 @@
+"""Python mirror of Acquisition.jl's public API over the C ABI (GB300 kernels underneath).
+
+Names, argument meaning and errors follow the reference:
+
+* ``plan_acquire``     — src/plan.jl:312-697
+* ``acquire_b``        — ``acquire!``, src/acquire.jl:54-89 and :788-797 (``!`` is spelled ``_b``)
+* ``acquire``          — src/acquire.jl:838-882
+* ``AcquisitionResults`` — src/Acquisition.jl:81-109
+* ``get_num_cells`` / ``is_detected`` — src/Acquisition.jl:124-142
+* ``cfar_threshold``   — src/cfar.jl:64-85
+* ``OppositeRowNoiseEstimator`` / ``GlobalMeanNoiseEstimator`` — src/est_signal_noise_power.jl:70,100
+
+Every acquisition runs on the GPU through libacqgb300.so; nothing here computes on the CPU
+beyond argument marshalling.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+
+
+class ArgumentError(ValueError):
+    """Mirror of Julia's ArgumentError (invalid plan or acquire! arguments)."""
+
+
+class AcquisitionError(RuntimeError):
+    """CUDA, allocation or device-wait failure inside the library."""
+
+
+def _check(status: int):
+    if status == L.ACQ_OK:
+        return
+    msg = L.last_error()
+    if status in (L.ACQ_ERR_ARGUMENT, L.ACQ_ERR_SHORT_SIGNAL, L.ACQ_ERR_PRN_NOT_IN_PLAN):
+        raise ArgumentError(msg)
+    raise AcquisitionError(f"status {status}: {msg}")
+
+
+# ---------------------------------------------------------------- systems and estimators
+@dataclass(frozen=True)
+class GNSSSystem:
+    name: str
+    sid: int
+    code_length: int
+    code_frequency: float
+    center_frequency: float
+    data_frequency: float
+    secondary_code: tuple = ()
+
+    @property
+    def secondary_code_length(self) -> int:
+        return max(1, len(self.secondary_code))
+
+    def gen_code(self, n: int, prn: int, sampling_freq: float, code_frequency: Optional[float] = None,
+                 start_phase: float = 0.0) -> np.ndarray:
+        """GNSSSignals ``gen_code`` semantics (host, C++)."""
+        out = np.empty(int(n), dtype=np.int8)
+        _check(L.load().acq_gen_code(self.sid, int(prn), int(n), float(sampling_freq),
+                                     float(code_frequency or 0.0), float(start_phase),
+                                     out.ctypes.data_as(C.POINTER(C.c_int8))))
+        return out
+
+
+_NH10 = (1, 1, 1, 1, -1, -1, 1, -1, 1, -1)
+
+
+def GPSL1CA() -> GNSSSystem:
+    return GNSSSystem("GPSL1CA", L.ACQ_GPS_L1CA, 1023, 1.023e6, 1575.42e6, 50.0)
+
+
+def GPSL5I() -> GNSSSystem:
+    return GNSSSystem("GPSL5I", L.ACQ_GPS_L5I, 10230, 10.23e6, 1176.45e6, 100.0, _NH10)
+
+
+def GalileoE1B() -> GNSSSystem:
+    """Galileo E1B with seeded synthetic memory codes and a BOC(1,1) sub-carrier."""
+    return GNSSSystem("GalileoE1B", L.ACQ_GALILEO_E1B, 4092, 1.023e6, 1575.42e6, 250.0)
+
+
+class AbstractNoiseEstimator:
+    code = -1
+
+
+class OppositeRowNoiseEstimator(AbstractNoiseEstimator):
+    code = L.ACQ_NOISE_OPPOSITE_ROW
+
+
+class GlobalMeanNoiseEstimator(AbstractNoiseEstimator):
+    code = L.ACQ_NOISE_GLOBAL_MEAN
+
+
+# ---------------------------------------------------------------- results
+@dataclass
+class AcquisitionResults:
+    system: GNSSSystem
+    prn: int
+    sampling_frequency: float
+    carrier_doppler: float
+    code_phase: float
+    secondary_code_phase: Optional[int]
+    CN0: float
+    noise_power: np.float32
+    peak_to_noise_ratio: np.float32
+    num_noncoherent_integrations: int
+    power_bins: Optional[np.ndarray]
+    dopplers: np.ndarray
+    num_blocks: int
+    block_size: int
+    num_secondary_rotations: int
+    # decision indices reported by the GPU pipeline (0-based)
+    peak_power: np.float32 = np.float32(0)
+    peak_doppler_bin: int = 0
+    peak_code_bin: int = 0
+    sign_pattern: int = -1
+    bit_edge: int = -1
+
+    def __repr__(self):
+        return (f"AcquisitionResults: PRN {self.prn}, CN0 = {self.CN0:.2f} dB-Hz, Doppler = "
+                f"{self.carrier_doppler} Hz, Code phase = {self.code_phase:.3f} chips")
+
+
+def get_num_cells(result: AcquisitionResults) -> int:
+    """src/Acquisition.jl:124-126."""
+    return len(result.dopplers) * result.num_blocks * result.block_size * result.num_secondary_rotations
+
+
+def cfar_threshold(pfa: float, num_cells: int, num_noncoherent_integrations: int = 1) -> float:
+    """src/cfar.jl:64-85 (host C++)."""
+    out = C.c_double()
+    _check(L.load().acq_cfar_threshold(float(pfa), int(num_cells), int(num_noncoherent_integrations),
+                                       C.byref(out)))
+    return out.value
+
+
+def is_detected(result: AcquisitionResults, pfa: float = 0.01) -> bool:
+    """src/Acquisition.jl:135-142."""
+    return float(result.peak_to_noise_ratio) > cfar_threshold(pfa, get_num_cells(result),
+                                                              result.num_noncoherent_integrations)
+
+
+# ---------------------------------------------------------------- plan
+def _desc(system: GNSSSystem, sampling_freq, min_doppler_coverage, n_coh, n_be, n_nc, noise_estimator,
+          use_secondary_code, max_rot, device) -> L.PlanDesc:
+    d = L.PlanDesc()
+    L.load().acq_plan_desc_init(C.byref(d))
+    d.system = system.sid
+    d.sampling_freq_hz = float(sampling_freq)
+    d.min_doppler_coverage_hz = float(min_doppler_coverage)
+    d.num_coherently_integrated_code_periods = int(n_coh)
+    d.bit_edge_search_steps = int(n_be)
+    d.num_noncoherent_accumulations = int(n_nc)
+    est = noise_estimator() if isinstance(noise_estimator, type) else noise_estimator
+    d.noise_estimator = est.code
+    d.use_secondary_code = 1 if use_secondary_code else 0
+    d.max_secondary_code_rotations = int(max_rot)
+    d.device = int(device)
+    return d
+
+
+def plan_geometry(system: GNSSSystem, sampling_freq, **kw) -> L.Geometry:
+    """Validation + geometry only (no GPU), the first half of plan_acquire."""
+    d = _desc(system, sampling_freq, kw.get("min_doppler_coverage", 7000.0),
+              kw.get("num_coherently_integrated_code_periods", 1), kw.get("bit_edge_search_steps", 1),
+              kw.get("num_noncoherent_accumulations", 1), kw.get("noise_estimator", OppositeRowNoiseEstimator()),
+              kw.get("use_secondary_code", True), kw.get("max_secondary_code_rotations", 32), kw.get("device", 0))
+    g = L.Geometry()
+    _check(L.load().acq_plan_query(C.byref(d), C.byref(g)))
+    return g
+
+
+class AcquisitionPlan:
+    """Pre-computed FM-DBZP plan (src/plan.jl:81-174) owning its device memory and stream."""
+
+    def __init__(self, system: GNSSSystem, sampling_freq: float, prns, desc: L.PlanDesc, codes=None):
+        lib = L.load()
+        self.system = system
+        self.sampling_freq = float(sampling_freq)
+        self.avail_prns = [int(p) for p in prns]
+        arr = (C.c_int32 * len(self.avail_prns))(*self.avail_prns)
+        codes_ptr = None
+        if codes is not None:
+            codes = np.ascontiguousarray(codes, dtype=np.int8)
+            codes_ptr = codes.ctypes.data_as(C.POINTER(C.c_int8))
+        h = C.c_void_p()
+        _check(lib.acq_plan_create(C.byref(desc), arr, len(self.avail_prns), codes_ptr, C.byref(h)))
+        self._h = h
+        g = L.Geometry()
+        _check(lib.acq_plan_get_geometry(h, C.byref(g)))
+        self.geometry = g
+        dop = np.empty(g.num_doppler_bins, dtype=np.float64)
+        _check(lib.acq_plan_doppler_freqs(h, dop.ctypes.data_as(C.POINTER(C.c_double))))
+        self.doppler_freqs = dop
+        self.noise_estimator = desc.noise_estimator
+        self.use_secondary_code = bool(desc.use_secondary_code)
+        self.max_secondary_code_rotations = desc.max_secondary_code_rotations
+        self.device = desc.device
+        # per-PRN cached power-bin matrices (src/plan.jl:123-126): lazily allocated, reused
+        self.result_buffers = [None] * len(self.avail_prns)
+
+    # geometry fields under the reference's names
+    samples_per_code = property(lambda s: s.geometry.samples_per_code)
+    samples_per_code_eff = property(lambda s: s.geometry.samples_per_code_eff)
+    num_blocks = property(lambda s: s.geometry.num_blocks)
+    block_size = property(lambda s: s.geometry.block_size)
+    fft_size = property(lambda s: s.geometry.fft_size)
+    num_coherently_integrated_code_periods = property(lambda s: s.geometry.num_coherently_integrated_code_periods)
+    num_data_bits = property(lambda s: s.geometry.num_data_bits)
+    bit_edge_search_steps = property(lambda s: s.geometry.bit_edge_search_steps)
+    num_noncoherent_accumulations = property(lambda s: s.geometry.num_noncoherent_accumulations)
+    num_secondary_rotations = property(lambda s: s.geometry.num_secondary_rotations)
+    num_doppler_bins = property(lambda s: s.geometry.num_doppler_bins)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def stream_handle(self) -> int:
+        s = C.c_void_p()
+        _check(L.load().acq_plan_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def last_launch_count(self) -> int:
+        n = C.c_int64()
+        _check(L.load().acq_plan_last_launch_count(self._h, C.byref(n)))
+        return n.value
+
+    def set_kernel_timing(self, enable: bool = True):
+        _check(L.load().acq_plan_set_kernel_timing(self._h, 1 if enable else 0))
+
+    def reset_kernel_times(self):
+        _check(L.load().acq_plan_reset_kernel_times(self._h))
+
+    def kernel_times(self) -> dict:
+        """{kernel class: (total device ms, launches)} accumulated since the last reset."""
+        ms = (C.c_double * L.KERNEL_KINDS)()
+        n = (C.c_int64 * L.KERNEL_KINDS)()
+        _check(L.load().acq_plan_kernel_times(self._h, ms, n, L.KERNEL_KINDS))
+        return {L.KERNEL_NAMES[i]: (ms[i], n[i]) for i in range(L.KERNEL_KINDS) if n[i] > 0}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().acq_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plan_acquire(system: GNSSSystem, sampling_freq, prns, *, min_doppler_coverage=7000.0,
+                 num_coherently_integrated_code_periods: int = 1, bit_edge_search_steps: int = 1,
+                 num_noncoherent_accumulations: int = 1, noise_estimator=OppositeRowNoiseEstimator(),
+                 use_secondary_code: bool = True, max_secondary_code_rotations: int = 32, device: int = 0,
+                 codes=None, fft_flag=None) -> AcquisitionPlan:
+    """plan_acquire (src/plan.jl:312-697). ``fft_flag`` is accepted and ignored (no FFTW)."""
+    d = _desc(system, sampling_freq, min_doppler_coverage, num_coherently_integrated_code_periods,
+              bit_edge_search_steps, num_noncoherent_accumulations, noise_estimator, use_secondary_code,
+              max_secondary_code_rotations, device)
+    return AcquisitionPlan(system, sampling_freq, list(np.atleast_1d(prns)), d, codes)
+
+
+# ---------------------------------------------------------------- acquire!
+def _as_samples(signal):
+    """Return (contiguous array, dtype code, n_samples) for a host signal."""
+    a = np.asarray(signal)
+    if np.iscomplexobj(a):
+        if a.dtype == np.complex64:
+            return np.ascontiguousarray(a), L.ACQ_CF32, a.size
+        if a.dtype == np.complex128:
+            return np.ascontiguousarray(a), L.ACQ_CF64, a.size
+        a = a.astype(np.complex64)
+        return np.ascontiguousarray(a), L.ACQ_CF32, a.size
+    if a.ndim >= 1 and a.shape[-1] == 2 and a.dtype in (np.int16, np.int8, np.float32, np.float64):
+        code = {np.dtype(np.int16): L.ACQ_CI16, np.dtype(np.int8): L.ACQ_CI8,
+                np.dtype(np.float32): L.ACQ_CF32, np.dtype(np.float64): L.ACQ_CF64}[a.dtype]
+        return np.ascontiguousarray(a), code, a.size // 2
+    if a.dtype.kind in "fiu":  # real samples -> ComplexF32(x)
+        return np.ascontiguousarray(a.astype(np.complex64)), L.ACQ_CF32, a.size
+    raise ArgumentError(f"unsupported signal dtype {a.dtype}")
+
+
+def _results(plan: AcquisitionPlan, res_arr, prns, store_power_bins, bins):
+    g = plan.geometry
+    out = []
+    for i, prn in enumerate(prns):
+        r = res_arr[i]
+        pb = None
+        if store_power_bins:
+            slot = plan.avail_prns.index(prn)
+            if plan.result_buffers[slot] is None:
+                plan.result_buffers[slot] = np.empty((g.num_doppler_bins, g.samples_per_code_eff), np.float32)
+            np.copyto(plan.result_buffers[slot], bins[i])
+            pb = plan.result_buffers[slot]
+        out.append(AcquisitionResults(
+            plan.system, int(r.prn), plan.sampling_freq, float(r.carrier_doppler_hz), float(r.code_phase),
+            None if r.secondary_code_phase < 0 else int(r.secondary_code_phase), float(r.cn0_dbhz),
+            np.float32(r.noise_power), np.float32(r.peak_to_noise_ratio), int(r.num_noncoherent_integrations),
+            pb, plan.doppler_freqs, g.num_blocks, g.block_size, g.num_secondary_rotations,
+            np.float32(r.peak_power), int(r.peak_doppler_bin), int(r.peak_code_bin), int(r.sign_pattern),
+            int(r.bit_edge)))
+    return out
+
+
+def _flags(subsample_interpolation, store_power_bins):
+    return ((L.ACQ_FLAG_SUBSAMPLE_INTERP if subsample_interpolation else 0)
+            | (L.ACQ_FLAG_STORE_POWER_BINS if store_power_bins else 0))
+
+
+def acquire_b(plan: AcquisitionPlan, signal, prns, *, interm_freq: float = 0.0,
+              subsample_interpolation: bool = False, store_power_bins: bool = False):
+    """``acquire!(plan, signal, prns; interm_freq, subsample_interpolation, store_power_bins)``.
+
+    ``signal`` is a host array (complex64/complex128, or (..., 2) int16/int8 interleaved) or a
+    CUDA tensor (see :func:`acquire_device`). A scalar ``prns`` returns one result.
+    """
+    single = np.ndim(prns) == 0
+    prn_list = [int(p) for p in np.atleast_1d(prns)]
+    if _is_cuda_tensor(signal):
+        out = acquire_device(plan, signal, prn_list, interm_freq=interm_freq,
+                             subsample_interpolation=subsample_interpolation, store_power_bins=store_power_bins)
+        return out[0] if single else out
+    lib = L.load()
+    arr, dt, n = _as_samples(signal)
+    g = plan.geometry
+    res = (L.Result * len(prn_list))()
+    bins = None
+    bins_ptr = None
+    if store_power_bins:
+        bins = np.empty((len(prn_list), g.num_doppler_bins, g.samples_per_code_eff), np.float32)
+        bins_ptr = bins.ctypes.data_as(C.POINTER(C.c_float))
+    prn_arr = (C.c_int32 * len(prn_list))(*prn_list)
+    _check(lib.acq_acquire(plan.handle, arr.ctypes.data_as(C.c_void_p), dt, int(n), prn_arr, len(prn_list),
+                           float(interm_freq), _flags(subsample_interpolation, store_power_bins), res, bins_ptr))
+    out = _results(plan, res, prn_list, store_power_bins, bins)
+    return out[0] if single else out
+
+
+def _is_cuda_tensor(x) -> bool:
+    return hasattr(x, "is_cuda") and hasattr(x, "data_ptr") and bool(x.is_cuda)
+
+
+def _tensor_dtype(t):
+    import torch
+    if t.dtype == torch.complex64:
+        return L.ACQ_CF32, t.numel()
+    if t.dtype == torch.complex128:
+        return L.ACQ_CF64, t.numel()
+    if t.shape[-1] == 2 and t.dtype in (torch.int16, torch.int8, torch.float32, torch.float64):
+        return {torch.int16: L.ACQ_CI16, torch.int8: L.ACQ_CI8, torch.float32: L.ACQ_CF32,
+                torch.float64: L.ACQ_CF64}[t.dtype], t.numel() // 2
+    raise ArgumentError(f"unsupported tensor dtype {t.dtype}")
+
+
+def acquire_device_async(plan: AcquisitionPlan, tensor, prns, *, interm_freq: float = 0.0,
+                         subsample_interpolation: bool = False, store_power_bins: bool = False):
+    """Enqueue an acquisition on the plan's stream for a device-resident signal (no wait)."""
+    if not tensor.is_contiguous():
+        raise ArgumentError("device signal must be contiguous")
+    dt, n = _tensor_dtype(tensor)
+    prn_list = [int(p) for p in np.atleast_1d(prns)]
+    prn_arr = (C.c_int32 * len(prn_list))(*prn_list)
+    _check(L.load().acq_acquire_device_async(plan.handle, C.c_void_p(tensor.data_ptr()), dt, int(n), prn_arr,
+                                             len(prn_list), float(interm_freq),
+                                             _flags(subsample_interpolation, store_power_bins)))
+    return prn_list
+
+
+def fetch_results(plan: AcquisitionPlan, prns, store_power_bins: bool = False):
+    g = plan.geometry
+    prn_list = [int(p) for p in np.atleast_1d(prns)]
+    res = (L.Result * len(prn_list))()
+    bins = None
+    bins_ptr = None
+    if store_power_bins:
+        bins = np.empty((len(prn_list), g.num_doppler_bins, g.samples_per_code_eff), np.float32)
+        bins_ptr = bins.ctypes.data_as(C.POINTER(C.c_float))
+    _check(L.load().acq_fetch_results(plan.handle, res, bins_ptr))
+    return _results(plan, res, prn_list, store_power_bins, bins)
+
+
+def acquire_device(plan: AcquisitionPlan, tensor, prns, *, interm_freq: float = 0.0,
+                   subsample_interpolation: bool = False, store_power_bins: bool = False):
+    """acquire! on a device-resident signal (a contiguous CUDA tensor)."""
+    import torch
+    torch.cuda.current_stream(tensor.device).synchronize()
+    prn_list = acquire_device_async(plan, tensor, prns, interm_freq=interm_freq,
+                                    subsample_interpolation=subsample_interpolation,
+                                    store_power_bins=store_power_bins)
+    return fetch_results(plan, prn_list, store_power_bins)
+
+
+def acquire(system: GNSSSystem, signal, sampling_freq, prns, *, interm_freq: float = 0.0,
+            min_doppler_coverage=7000.0, num_coherently_integrated_code_periods: int = 1,
+            bit_edge_search_steps: int = 1, num_noncoherent_accumulations: int = 1,
+            use_secondary_code: bool = True, max_secondary_code_rotations: int = 32,
+            noise_estimator=OppositeRowNoiseEstimator(), subsample_interpolation: bool = False,
+            store_power_bins: bool = False, fft_flag=None, device: int = 0):
+    """acquire (src/acquire.jl:838-882): plan_acquire then acquire!."""
+    single = np.ndim(prns) == 0
+    prn_list = [int(p) for p in np.atleast_1d(prns)]
+    plan = plan_acquire(system, sampling_freq, prn_list, min_doppler_coverage=min_doppler_coverage,
+                        num_coherently_integrated_code_periods=num_coherently_integrated_code_periods,
+                        bit_edge_search_steps=bit_edge_search_steps,
+                        num_noncoherent_accumulations=num_noncoherent_accumulations,
+                        noise_estimator=noise_estimator, use_secondary_code=use_secondary_code,
+                        max_secondary_code_rotations=max_secondary_code_rotations, device=device)
+    try:
+        out = acquire_b(plan, signal, prn_list, interm_freq=interm_freq,
+                        subsample_interpolation=subsample_interpolation, store_power_bins=store_power_bins)
+    finally:
+        if not store_power_bins:
+            plan.close()
+    return out[0] if single else out

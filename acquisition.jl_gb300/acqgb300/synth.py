@@ -1,0 +1,91 @@
+"""Seeded synthetic GNSS recordings (host, numpy) following the reference's signal model.
+
+Model (src/generate_test_signal.jl:45-68): per satellite, the code sampled at the Doppler-
+shifted code rate f_code + f_d * f_code / f_carrier with GNSSSignals ``gen_code`` semantics,
+times the carrier exp(i(2 pi (IF + f_d) t + phi0)), times +-1 data bits; plus complex white
+Gaussian noise with the statistics of Julia's ``randn(ComplexF64)`` (unit total variance).
+
+Scaling: noise has unit total power; a satellite at C/N0 (dB-Hz) has amplitude
+sqrt(10^(CN0/10) / fs) — the reference's ``unit_noise_power = true`` convention.
+
+Quantisers: ``to_ci16`` (x * 2^10, round, saturate) and ``to_ci8_3bit`` (3-bit, levels
++-1..+-7 at 0.5 sigma per component). Codes come from the C++ generator of libacqgb300.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .api import GNSSSystem
+
+
+@dataclass
+class Satellite:
+    prn: int
+    cn0: float                   # dB-Hz
+    doppler: float               # Hz
+    code_phase: float            # chips
+    phase: float = math.pi / 8   # carrier phase offset, rad
+    data_bits: bool = True       # +-1 data bits at the system's data rate
+    bit_offset: float = 0.0      # seconds into the first data bit at sample 0
+
+
+@dataclass
+class Recording:
+    system: GNSSSystem
+    fs: float
+    samples: np.ndarray           # complex64 (or quantised, see `quantised`)
+    sats: list = field(default_factory=list)
+    interm_freq: float = 0.0
+
+
+def synth(system: GNSSSystem, fs: float, n: int, sats, seed: int, interm_freq: float = 0.0,
+          noise: bool = True) -> np.ndarray:
+    """complex128 samples of the model above."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(n, dtype=np.float64)
+    out = np.zeros(n, dtype=np.complex128)
+    for s in sats:
+        fc = system.code_frequency + s.doppler * system.code_frequency / system.center_frequency
+        code = system.gen_code(n, s.prn, fs, fc, s.code_phase).astype(np.float64)
+        carrier = np.exp(1j * (2 * math.pi * t * (interm_freq + s.doppler) / fs + s.phase))
+        amp = math.sqrt(10 ** (s.cn0 / 10) / fs)
+        x = amp * code * carrier
+        if s.data_bits and math.isfinite(system.data_frequency) and system.data_frequency > 0:
+            bit_idx = np.floor((t / fs + s.bit_offset) * system.data_frequency).astype(np.int64)
+            nb = int(bit_idx[-1]) + 1
+            bits = rng.choice(np.array([-1.0, 1.0]), size=nb)
+            x = x * bits[bit_idx]
+        out += x
+    if noise:
+        out += (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / math.sqrt(2)
+    return out
+
+
+def to_ci16(x: np.ndarray, scale: float = 2.0 ** 10) -> np.ndarray:
+    """Interleaved int16 (n, 2): round(x * scale), saturated."""
+    re = np.clip(np.rint(x.real * scale), -32768, 32767)
+    im = np.clip(np.rint(x.imag * scale), -32768, 32767)
+    return np.stack([re, im], axis=-1).astype(np.int16)
+
+
+def to_ci8_3bit(x: np.ndarray) -> np.ndarray:
+    """Interleaved int8 (n, 2): 3-bit quantiser, odd levels -7..7, step 0.5 sigma per component."""
+    sigma = math.sqrt(0.5)
+
+    def q(v):
+        k = np.floor(v / (0.5 * sigma))
+        return np.clip(2 * k + 1, -7, 7)
+
+    return np.stack([q(x.real), q(x.imag)], axis=-1).astype(np.int8)
+
+
+def random_sats(rng: np.random.Generator, prns, cn0_range, doppler_max, code_length, bit_period_s=0.0):
+    out = []
+    for prn in prns:
+        out.append(Satellite(int(prn), float(rng.uniform(*cn0_range)), float(rng.uniform(-doppler_max, doppler_max)),
+                             float(rng.uniform(0, code_length)), float(rng.uniform(0, 2 * math.pi)), True,
+                             float(rng.uniform(0, bit_period_s)) if bit_period_s > 0 else 0.0))
+    return out

@@ -1,0 +1,67 @@
+"""Build libacqgb300.so in-tree (sm_103a only).
+
+    python acquisition.jl_gb300/build_lib.py [--debug]
+
+Compiles the host C++ (g++) and the CUDA runtime/kernels (nvcc) in parallel and links
+``acquisition.jl_gb300/acqgb300/libacqgb300.so``. No cmake. Host code is compiled with
+-ffp-contract=off so double-precision geometry rounds identically on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+OUT_DIR = os.path.join(HERE, "acqgb300")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT_DIR, "libacqgb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for c in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stdout + r.stderr
+
+
+def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    opt = ["-O0", "-g"] if debug else ["-O3"]
+    host_obj = os.path.join(BUILD_DIR, "acq_host.o")
+    dev_obj = os.path.join(BUILD_DIR, "acq_runtime.o")
+    host_cmd = ["g++", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", *opt,
+                f"-I{INCLUDE}", "-c", os.path.join(CSRC, "acq_host.cpp"), "-o", host_obj]
+    dev_cmd = [nvcc, "-std=c++17", *ARCH, "-lineinfo", *opt, "-Xcompiler", "-fPIC,-ffp-contract=off",
+               f"-I{INCLUDE}", f"-I{CSRC}", "-c", os.path.join(CSRC, "acq_runtime.cu"), "-o", dev_obj]
+    if ptxas_verbose:
+        dev_cmd.insert(1, "-Xptxas=-v")
+    with ThreadPoolExecutor(2) as ex:
+        outs = list(ex.map(_run, [host_cmd, dev_cmd]))
+    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, "-o", LIB + ".tmp", "-lcudart_static", "-lrt", "-ldl",
+                "-lpthread"]
+    outs.append(_run(link_cmd))
+    os.replace(LIB + ".tmp", LIB)
+    log = "".join(outs)
+    if verbose:
+        print(log)
+    return log
+
+
+if __name__ == "__main__":
+    print(build(verbose=False, debug="--debug" in sys.argv, ptxas_verbose="-v" in sys.argv))
+    print("built", LIB)

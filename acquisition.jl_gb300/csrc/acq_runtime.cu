@@ -1,0 +1,620 @@
+// acq_runtime.cu — plan lifetime, device memory, launch sequence and the C ABI of
+// libacqgb300. Host logic mirrors plan_acquire / acquire! (src/plan.jl:312-697,
+// src/acquire.jl:54-215); all per-sample work runs in the kernels of acq_kernels.cuh.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "acq_host.h"
+#include "acq_kernels.cuh"
+
+using namespace acq;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct CudaError : AcqError {
+    explicit CudaError(const std::string& m) : AcqError(ACQ_ERR_CUDA, m) {}
+};
+
+#define CK(x)                                                                                        \
+    do {                                                                                             \
+        cudaError_t e_ = (x);                                                                        \
+        if (e_ != cudaSuccess)                                                                       \
+            throw CudaError(std::string(#x) + ": " + cudaGetErrorName(e_) + " " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kThreads = 256;
+constexpr size_t kSmemBudget = 200 * 1024;   // dynamic shared memory per CTA we plan for
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void reset() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t n) {
+        if (n <= bytes) return;
+        reset();
+        if (n == 0) return;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw AcqError(ACQ_ERR_ALLOC, "cudaMalloc(" + std::to_string(n) + ") failed: " + cudaGetErrorString(e));
+        }
+        bytes = n;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+FftDesc make_fft_desc(int n, DevBuf& tw) {
+    FftDesc d{};
+    d.n = n;
+    std::vector<int> r = fft_radices(n);
+    if (static_cast<int>(r.size()) > kMaxFftStages) throw AcqError(ACQ_ERR_UNSUPPORTED, "FFT has too many stages");
+    d.nst = static_cast<int>(r.size());
+    int ns = 1;
+    for (int s = 0; s < d.nst; ++s) {
+        d.radix[s] = r[s];
+        d.ns[s] = ns;
+        d.stride[s] = n / (ns * r[s]);
+        ns *= r[s];
+    }
+    std::vector<float2> h(n);
+    for (int k = 0; k < n; ++k) {
+        // exp(-2 pi i k / n) from a reduced angle, computed in double then rounded
+        double a = -2.0 * M_PI * static_cast<double>(k) / static_cast<double>(n);
+        h[k] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+    }
+    tw.ensure(sizeof(float2) * n);
+    CK(cudaMemcpy(tw.p, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    d.tw = tw.as<float2>();
+    return d;
+}
+
+int pow2_floor(int x) {
+    int p = 1;
+    while (p * 2 <= x) p *= 2;
+    return p;
+}
+
+size_t sample_bytes(int dtype) {
+    switch (dtype) {
+        case ACQ_CF32: return 8;
+        case ACQ_CI16: return 4;
+        case ACQ_CI8: return 2;
+        case ACQ_CF64: return 16;
+        default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown sample dtype " + std::to_string(dtype));
+    }
+}
+
+}  // namespace
+
+struct acq_plan {
+    acq_plan_desc desc{};
+    Geometry g{};
+    const SystemInfo* sys = nullptr;
+    std::vector<int> prns;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    FftDesc fftF{}, fftD{};
+    DevBuf twF, twD;
+    // plan-time constants
+    DevBuf codes, conj, chips, pats, drift, sec, if_off;
+    int64_t chips_len = 0;
+    int n_pat = 1, combos = 1, edge_step = 1;
+    // per-acquisition buffers
+    DevBuf input, S, T, accb, winb, rowpart, colsum, peakpart, zs, res, slots, prn_ids;
+    int tileB = 1, Wsimple = 1, Wsign = 1, nct = 1;
+    size_t smem_front = 0, smem_tile = 0, smem_simple = 0, smem_sign = 0;
+    // last acquisition
+    int last_n = 0;
+    uint32_t last_flags = 0;
+    int64_t launches = 0;
+    std::vector<int> req_prns;
+    // optional per-launch timing (acq_plan_set_kernel_timing)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_start, ev_stop;
+    std::vector<int> ev_kind;
+    size_t ev_used = 0;
+    double kt_ms[ACQ_KERNEL_KINDS] = {0};
+    int64_t kt_n[ACQ_KERNEL_KINDS] = {0};
+};
+
+namespace {
+
+// Allow every kernel the opt-in maximum once (per device); the launch decides what it uses,
+// so plans with different shapes never shrink each other's limit.
+constexpr int kSmemOptIn = 227 * 1024;
+void set_smem(const void* fn, size_t bytes) {
+    if (bytes > static_cast<size_t>(kSmemOptIn))
+        throw AcqError(ACQ_ERR_UNSUPPORTED, "kernel needs " + std::to_string(bytes) + " bytes of shared memory");
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemOptIn));
+}
+
+void t_begin(acq_plan* P, int kind) {
+    if (!P->timing) return;
+    if (P->ev_used == P->ev_start.size()) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        P->ev_start.push_back(a);
+        P->ev_stop.push_back(b);
+        P->ev_kind.push_back(kind);
+    }
+    P->ev_kind[P->ev_used] = kind;
+    CK(cudaEventRecord(P->ev_start[P->ev_used], P->stream));
+}
+
+void t_end(acq_plan* P) {
+    if (!P->timing) return;
+    CK(cudaEventRecord(P->ev_stop[P->ev_used], P->stream));
+    ++P->ev_used;
+}
+
+void t_collect(acq_plan* P) {
+    for (size_t i = 0; i < P->ev_used; ++i) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, P->ev_start[i], P->ev_stop[i]));
+        P->kt_ms[P->ev_kind[i]] += ms;
+        P->kt_n[P->ev_kind[i]] += 1;
+    }
+    P->ev_used = 0;
+}
+
+void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
+    const Geometry& g = P->g;
+    CK(cudaSetDevice(P->device));
+    CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    P->fftF = make_fft_desc(g.fft_size, P->twF);
+    P->fftD = make_fft_desc(g.ndop, P->twD);
+    // launch shapes
+    P->smem_front = 2 * sizeof(float2) * g.fft_size;
+    if (P->smem_front > kSmemBudget)
+        throw AcqError(ACQ_ERR_UNSUPPORTED, "fft_size=" + std::to_string(g.fft_size) + " exceeds shared memory");
+    P->tileB = std::max(1, std::min(8, static_cast<int>((96 * 1024 / (sizeof(float2) * g.fft_size) - 1) / 2)));
+    P->smem_tile = sizeof(float2) * g.fft_size * (1 + 2 * P->tileB);
+    P->Wsimple = std::max(1, std::min(32, pow2_floor(static_cast<int>(kSmemBudget / (16 * (size_t)g.ndop)))));
+    if (16ull * g.ndop > kSmemBudget) throw AcqError(ACQ_ERR_UNSUPPORTED, "num_doppler_bins too large");
+    P->smem_simple = 16ull * g.ndop * P->Wsimple;
+    const size_t per_col_sign = 3 * 8 + 4 + 2;  // tile + 2 work buffers + stage + winner, per row
+    P->Wsign = std::max(1, std::min(16, pow2_floor(static_cast<int>(kSmemBudget / (per_col_sign * g.ndop + 8)))));
+    if (per_col_sign * g.ndop + 8 > kSmemBudget) throw AcqError(ACQ_ERR_UNSUPPORTED, "num_doppler_bins too large");
+    P->smem_sign = per_col_sign * (size_t)g.ndop * P->Wsign + 4 * P->Wsign + 16;
+    set_smem((const void*)k_frontend, P->smem_front);
+    set_smem((const void*)k_code_spectra, P->smem_front);
+    set_smem((const void*)k_tile, P->smem_tile);
+    set_smem((const void*)k_col_simple, P->smem_simple);
+    set_smem((const void*)k_col_sign, P->smem_sign);
+    set_smem((const void*)k_col_rot, P->smem_sign);
+    P->nct = (g.spc_eff + kStatsCols - 1) / kStatsCols;
+
+    // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
+    std::vector<int8_t> h_codes(static_cast<size_t>(n_prns) * g.spc);
+    for (int i = 0; i < n_prns; ++i) {
+        if (user_codes)
+            std::memcpy(&h_codes[(size_t)i * g.spc], user_codes + (size_t)i * g.spc, g.spc);
+        else
+            gen_code(P->desc.system, prns[i], g.spc, P->desc.sampling_freq_hz, 0.0, 0.0, &h_codes[(size_t)i * g.spc]);
+    }
+    P->codes.ensure(h_codes.size());
+    CK(cudaMemcpy(P->codes.p, h_codes.data(), h_codes.size(), cudaMemcpyHostToDevice));
+    P->conj.ensure(sizeof(float2) * (size_t)n_prns * g.nb * g.fft_size);
+    k_code_spectra<<<n_prns * g.nb, kThreads, P->smem_front, P->stream>>>(P->codes.as<int8_t>(), g.spc, g.nb, g.bs,
+                                                                           P->fftF, P->conj.as<float2>());
+    CK(cudaGetLastError());
+    // full chip tables for the secondary-code despread (rotation path only)
+    if (g.path == 2) {
+        std::vector<int8_t> c0 = full_chips(P->desc.system, prns[0]);
+        P->chips_len = static_cast<int64_t>(c0.size());
+        std::vector<int8_t> all((size_t)n_prns * P->chips_len);
+        for (int i = 0; i < n_prns; ++i) {
+            std::vector<int8_t> c = full_chips(P->desc.system, prns[i]);
+            std::memcpy(&all[(size_t)i * P->chips_len], c.data(), P->chips_len);
+        }
+        P->chips.ensure(all.size());
+        CK(cudaMemcpy(P->chips.p, all.data(), all.size(), cudaMemcpyHostToDevice));
+        P->sec.ensure(P->sys->secondary_length);
+        CK(cudaMemcpy(P->sec.p, P->sys->secondary, P->sys->secondary_length, cudaMemcpyHostToDevice));
+    }
+    // sign patterns per PRN, src/sign_patterns.jl:23-47
+    if (g.path != 0) {
+        P->combos = 1 << (g.ndb - 1);
+        std::vector<float> all;
+        for (int i = 0; i < n_prns; ++i) {
+            std::vector<float> p = sign_patterns(P->desc.system, prns[i], g.ndb, g.R, g.n_coh, g.use_secondary_code != 0);
+            P->n_pat = static_cast<int>(p.size() / g.n_coh);
+            all.insert(all.end(), p.begin(), p.end());
+        }
+        P->pats.ensure(sizeof(float) * all.size());
+        CK(cudaMemcpy(P->pats.p, all.data(), sizeof(float) * all.size(), cudaMemcpyHostToDevice));
+        const int bpc_k = g.n_coh / g.ndb;
+        P->edge_step = bpc_k * g.nb / g.n_be;   // src/acquire.jl:298-299
+    }
+    // drift shifts per step, src/noncoherent_integration.jl:600-619
+    std::vector<int32_t> dr((size_t)g.n_nc * g.ndop);
+    for (int m = 0; m < g.n_nc; ++m) code_drift_shifts(g, *P->sys, P->desc.sampling_freq_hz, m, &dr[(size_t)m * g.ndop]);
+    P->drift.ensure(sizeof(int32_t) * dr.size());
+    CK(cudaMemcpy(P->drift.p, dr.data(), sizeof(int32_t) * dr.size(), cudaMemcpyHostToDevice));
+    // per-acquisition buffers sized for all plan PRNs
+    const size_t np = n_prns;
+    P->S.ensure(sizeof(float2) * (size_t)g.n_nc * g.ndop * g.fft_size);
+    P->T.ensure(sizeof(float2) * np * g.ndop * g.spc);
+    P->accb.ensure(sizeof(float) * np * g.ndop * g.spc_eff);
+    if (g.path != 0) P->winb.ensure(sizeof(uint16_t) * np * g.ndop * g.spc_eff);
+    P->rowpart.ensure(sizeof(double) * np * P->nct * g.ndop);
+    P->colsum.ensure(sizeof(double) * np * g.spc_eff);
+    P->peakpart.ensure(sizeof(unsigned long long) * np * P->nct);
+    P->zs.ensure(sizeof(double2) * np * std::max(1, g.R));
+    P->res.ensure(sizeof(acq_result) * np);
+    P->slots.ensure(sizeof(int) * np);
+    P->prn_ids.ensure(sizeof(int) * np);
+    P->if_off.ensure(sizeof(float) * g.n_nc);
+    CK(cudaStreamSynchronize(P->stream));
+}
+
+void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples, const int32_t* prns, int n,
+                     double interm_freq, uint32_t flags) {
+    const Geometry& g = P->g;
+    const int64_t seg_len = static_cast<int64_t>(g.n_coh) * g.spc;
+    // src/acquire.jl:62-72
+    std::vector<int> slots(n);
+    for (int i = 0; i < n; ++i) {
+        auto it = std::find(P->prns.begin(), P->prns.end(), prns[i]);
+        if (it == P->prns.end()) {
+            std::string got = "[", av = "[";
+            for (int j = 0; j < n; ++j) got += (j ? ", " : "") + std::to_string(prns[j]);
+            for (size_t j = 0; j < P->prns.size(); ++j) av += (j ? ", " : "") + std::to_string(P->prns[j]);
+            throw AcqError(ACQ_ERR_PRN_NOT_IN_PLAN,
+                           "All requested PRNs must be in plan.avail_prns. Got: " + got + "], available: " + av + "]");
+        }
+        slots[i] = static_cast<int>(it - P->prns.begin());
+    }
+    const int64_t nseg = n_samples / seg_len;
+    if (nseg < g.n_nc)
+        throw AcqError(ACQ_ERR_SHORT_SIGNAL, "Signal has " + std::to_string(n_samples) + " samples → " +
+                                                 std::to_string(nseg) + " full segments of " + std::to_string(seg_len) +
+                                                 ", but plan.num_noncoherent_accumulations=" + std::to_string(g.n_nc) +
+                                                 ". Provide a longer signal.");
+    if (n <= 0) throw AcqError(ACQ_ERR_ARGUMENT, "no PRNs requested");
+    CK(cudaSetDevice(P->device));
+    cudaStream_t st = P->stream;
+    int64_t L = 0;
+    CK(cudaMemcpyAsync(P->slots.p, slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(P->prn_ids.p, prns, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    // IF wipe-off constants in FP32, src/acquire.jl:96-97
+    const int use_if = interm_freq != 0.0;
+    float if_step = 0.f;
+    std::vector<float> offs(g.n_nc, 0.f);
+    if (use_if) {
+        if_step = static_cast<float>(-2.0 * M_PI * interm_freq / P->desc.sampling_freq_hz);
+        for (int m = 0; m < g.n_nc; ++m) {
+            const float seg0 = static_cast<float>(static_cast<int64_t>(m) * seg_len);
+            volatile float prod = seg0 * if_step;
+            offs[m] = prod;
+        }
+        CK(cudaMemcpyAsync(P->if_off.p, offs.data(), sizeof(float) * g.n_nc, cudaMemcpyHostToDevice, st));
+    }
+    const int G = g.n_coh * g.nb;
+    t_begin(P, ACQ_KERNEL_FRONTEND);
+    k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF, P->S.as<float2>(),
+                                                            use_if, if_step, P->if_off.as<float>());
+    t_end(P);
+    ++L;
+    const float inv_F = 1.0f / static_cast<float>(g.fft_size);
+    for (int m = 0; m < g.n_nc; ++m) {
+        const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_size;
+        t_begin(P, ACQ_KERNEL_TILE);
+        k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb, g.bs,
+                                                           g.spc, P->fftF, P->tileB, inv_F, P->T.as<float2>());
+        t_end(P);
+        ++L;
+        const int* dr = P->drift.as<int>() + (size_t)m * g.ndop;
+        const int first = m == 0;
+        t_begin(P, ACQ_KERNEL_COLUMN);
+        if (g.path == 0) {
+            const int W = P->Wsimple;
+            k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
+                P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
+        } else if (g.path == 1) {
+            const int W = P->Wsign;
+            k_col_sign<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(
+                P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
+                P->edge_step, P->slots.as<int>(), dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+        } else {
+            const int W = P->Wsign;
+            const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            k_col_rot<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(
+                P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, P->pats.as<float>(), g.n_coh, g.nb, g.bs, g.R, P->combos,
+                g.n_be, P->edge_step, use_max, P->slots.as<int>(), dr, first, P->accb.as<float>(),
+                P->winb.as<uint16_t>(), g.spc_eff);
+        }
+        t_end(P);
+        ++L;
+    }
+    const int streamed_rot = (g.n_nc == 1 && g.R > 1) ? 1 : 0;
+    t_begin(P, ACQ_KERNEL_STATS);
+    k_stats<<<dim3(P->nct, n), kThreads, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc_eff, g.spc, g.R, streamed_rot,
+                                                  P->rowpart.as<double>(), P->colsum.as<double>(),
+                                                  P->peakpart.as<unsigned long long>());
+    t_end(P);
+    ++L;
+    ExtractParams EP{};
+    EP.ndop = g.ndop; EP.spc = g.spc; EP.spc_eff = g.spc_eff; EP.nb = g.nb; EP.bs = g.bs; EP.R = g.R;
+    EP.n_coh = g.n_coh; EP.ndb = g.ndb; EP.n_be = g.n_be; EP.n_nc = g.n_nc; EP.path = g.path;
+    EP.combos = P->combos; EP.n_pat = P->n_pat; EP.streamed_rot = streamed_rot;
+    EP.noise_estimator = g.noise_estimator;
+    EP.samples_per_chip = static_cast<int>(std::floor(P->desc.sampling_freq_hz / P->sys->code_freq));
+    EP.interp = (flags & ACQ_FLAG_SUBSAMPLE_INTERP) ? 1 : 0;
+    EP.nct = P->nct;
+    EP.fs = P->desc.sampling_freq_hz; EP.fc = P->sys->code_freq; EP.code_length = P->sys->code_length;
+    EP.t_coh = g.n_coh * (static_cast<double>(P->sys->code_length) / P->sys->code_freq);
+    EP.doppler_first = g.doppler_first; EP.doppler_step = g.doppler_step; EP.cfar_thr = g.cfar_thr;
+    t_begin(P, ACQ_KERNEL_EXTRACT);
+    k_extract<<<n, kThreads, 0, st>>>(P->accb.as<float>(), P->winb.as<uint16_t>(), P->rowpart.as<double>(),
+                                      P->colsum.as<double>(), P->peakpart.as<unsigned long long>(), P->prn_ids.as<int>(),
+                                      EP, P->res.as<acq_result>());
+    t_end(P);
+    ++L;
+    if (g.R > 1) {
+        t_begin(P, ACQ_KERNEL_SECONDARY);
+        k_secondary_prompt<<<dim3(n, g.R), kThreads, 0, st>>>(d_in, dtype, P->chips.as<int8_t>(), P->chips_len,
+                                                              P->slots.as<int>(), g.spc, P->desc.sampling_freq_hz,
+                                                              P->sys->code_freq, interm_freq, P->res.as<acq_result>(),
+                                                              P->zs.as<double2>(), g.R);
+        k_secondary_argmax<<<(n + 127) / 128, 128, 0, st>>>(P->zs.as<double2>(), P->sec.as<int8_t>(), g.R,
+                                                            P->res.as<acq_result>(), n);
+        t_end(P);
+        L += 2;
+    }
+    CK(cudaGetLastError());
+    P->launches = L;
+    P->last_n = n;
+    P->last_flags = flags;
+    P->req_prns.assign(prns, prns + n);
+}
+
+void fetch(acq_plan* P, acq_result* results, float* power_bins) {
+    const Geometry& g = P->g;
+    CK(cudaSetDevice(P->device));
+    if (results)
+        CK(cudaMemcpyAsync(results, P->res.p, sizeof(acq_result) * P->last_n, cudaMemcpyDeviceToHost, P->stream));
+    if (power_bins && (P->last_flags & ACQ_FLAG_STORE_POWER_BINS))
+        CK(cudaMemcpyAsync(power_bins, P->accb.p, sizeof(float) * (size_t)P->last_n * g.ndop * g.spc_eff,
+                           cudaMemcpyDeviceToHost, P->stream));
+    CK(cudaStreamSynchronize(P->stream));
+    t_collect(P);
+}
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return ACQ_OK;
+    } catch (const AcqError& e) {
+        g_last_error = e.what();
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return ACQ_ERR_ALLOC;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return ACQ_ERR_ARGUMENT;
+    }
+}
+
+void fill_geometry(const Geometry& g, const SystemInfo& s, int n_prns, acq_geometry* o) {
+    o->samples_per_code = g.spc;
+    o->samples_per_code_eff = g.spc_eff;
+    o->num_blocks = g.nb;
+    o->block_size = g.bs;
+    o->fft_size = g.fft_size;
+    o->num_coherently_integrated_code_periods = g.n_coh;
+    o->num_data_bits = g.ndb;
+    o->bit_edge_search_steps = g.n_be;
+    o->num_noncoherent_accumulations = g.n_nc;
+    o->num_doppler_bins = g.ndop;
+    o->num_secondary_rotations = g.R;
+    o->bit_period_codes = g.bit_period_codes;
+    o->num_prns = n_prns;
+    o->path = g.path;
+    o->doppler_first_hz = g.doppler_first;
+    o->doppler_step_hz = g.doppler_step;
+    o->code_length = s.code_length;
+    o->code_freq_hz = s.code_freq;
+    o->center_freq_hz = s.center_freq;
+    o->cfar_threshold_pfa001 = g.cfar_thr;
+}
+
+}  // namespace
+
+extern "C" {
+
+void acq_plan_desc_init(acq_plan_desc* d) {
+    if (!d) return;
+    d->system = ACQ_GPS_L1CA;
+    d->sampling_freq_hz = 0.0;
+    d->min_doppler_coverage_hz = 7000.0;
+    d->num_coherently_integrated_code_periods = 1;
+    d->bit_edge_search_steps = 1;
+    d->num_noncoherent_accumulations = 1;
+    d->noise_estimator = ACQ_NOISE_OPPOSITE_ROW;
+    d->use_secondary_code = 1;
+    d->max_secondary_code_rotations = 32;
+    d->device = 0;
+}
+
+int acq_plan_query(const acq_plan_desc* desc, acq_geometry* out) {
+    return guarded([&] {
+        if (!desc || !out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        Geometry g = compute_geometry(*desc);
+        fill_geometry(g, system_info(desc->system), 0, out);
+    });
+}
+
+int acq_plan_create(const acq_plan_desc* desc, const int32_t* prns, int32_t n_prns, const int8_t* codes, acq_plan** out) {
+    return guarded([&] {
+        if (!desc || !out || (!prns && n_prns > 0)) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        if (n_prns <= 0) throw AcqError(ACQ_ERR_ARGUMENT, "prns must not be empty");
+        std::unique_ptr<acq_plan> P(new acq_plan());
+        P->desc = *desc;
+        P->g = compute_geometry(*desc);
+        P->sys = &system_info(desc->system);
+        for (int i = 0; i < n_prns; ++i) {
+            if (prns[i] < 1 || prns[i] > P->sys->max_prn)
+                throw AcqError(ACQ_ERR_ARGUMENT, std::string(P->sys->name) + " PRN must be in 1:" +
+                                                     std::to_string(P->sys->max_prn) + ", got " + std::to_string(prns[i]));
+            P->prns.push_back(prns[i]);
+        }
+        P->device = desc->device;
+        try {
+            plan_setup(P.get(), prns, n_prns, codes);
+        } catch (...) {
+            acq_plan_destroy(P.release());
+            throw;
+        }
+        *out = P.release();
+    });
+}
+
+int acq_plan_destroy(acq_plan* P) {
+    if (!P) return ACQ_OK;
+    cudaSetDevice(P->device);
+    if (P->stream) cudaStreamSynchronize(P->stream);
+    for (DevBuf* b : {&P->twF, &P->twD, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
+                      &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
+                      &P->res, &P->slots, &P->prn_ids})
+        b->reset();
+    for (cudaEvent_t e : P->ev_start) cudaEventDestroy(e);
+    for (cudaEvent_t e : P->ev_stop) cudaEventDestroy(e);
+    if (P->stream) cudaStreamDestroy(P->stream);
+    delete P;
+    return ACQ_OK;
+}
+
+int acq_plan_get_geometry(const acq_plan* P, acq_geometry* out) {
+    return guarded([&] {
+        if (!P || !out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        fill_geometry(P->g, *P->sys, static_cast<int>(P->prns.size()), out);
+    });
+}
+
+int acq_plan_doppler_freqs(const acq_plan* P, double* out) {
+    return guarded([&] {
+        if (!P || !out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        std::memcpy(out, P->g.doppler_freqs.data(), sizeof(double) * P->g.ndop);
+    });
+}
+
+int acq_acquire(acq_plan* P, const void* samples, int32_t dtype, int64_t n_samples, const int32_t* prns,
+                int32_t n_prns, double interm_freq_hz, uint32_t flags, acq_result* results, float* power_bins) {
+    return guarded([&] {
+        if (!P || !samples || !prns || !results) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if ((flags & ACQ_FLAG_STORE_POWER_BINS) && !power_bins)
+            throw AcqError(ACQ_ERR_ARGUMENT, "store_power_bins requested without an output buffer");
+        const size_t eb = sample_bytes(dtype);
+        const Geometry& g = P->g;
+        // only the first N_nc segments are read (src/acquire.jl:65-72)
+        const int64_t need = static_cast<int64_t>(g.n_nc) * g.n_coh * g.spc;
+        const int64_t ncopy = std::min<int64_t>(n_samples, need);
+        CK(cudaSetDevice(P->device));
+        P->input.ensure(eb * std::max<int64_t>(ncopy, 1));
+        CK(cudaMemcpyAsync(P->input.p, samples, eb * ncopy, cudaMemcpyHostToDevice, P->stream));
+        enqueue_acquire(P, P->input.p, dtype, n_samples, prns, n_prns, interm_freq_hz, flags);
+        fetch(P, results, power_bins);
+    });
+}
+
+int acq_acquire_device_async(acq_plan* P, const void* d_samples, int32_t dtype, int64_t n_samples,
+                             const int32_t* prns, int32_t n_prns, double interm_freq_hz, uint32_t flags) {
+    return guarded([&] {
+        if (!P || !d_samples || !prns) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        sample_bytes(dtype);
+        enqueue_acquire(P, d_samples, dtype, n_samples, prns, n_prns, interm_freq_hz, flags);
+    });
+}
+
+int acq_fetch_results(acq_plan* P, acq_result* results, float* power_bins) {
+    return guarded([&] {
+        if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        fetch(P, results, power_bins);
+    });
+}
+
+int acq_plan_stream(const acq_plan* P, void** stream) {
+    return guarded([&] {
+        if (!P || !stream) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *stream = static_cast<void*>(P->stream);
+    });
+}
+
+int acq_plan_last_launch_count(const acq_plan* P, int64_t* count) {
+    return guarded([&] {
+        if (!P || !count) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *count = P->launches;
+    });
+}
+
+int acq_plan_set_kernel_timing(acq_plan* P, int32_t enable) {
+    return guarded([&] {
+        if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        P->timing = enable != 0;
+    });
+}
+
+int acq_plan_kernel_times(acq_plan* P, double* total_ms, int64_t* launches, int32_t n_kinds) {
+    return guarded([&] {
+        if (!P || !total_ms || !launches) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        for (int i = 0; i < n_kinds && i < ACQ_KERNEL_KINDS; ++i) {
+            total_ms[i] = P->kt_ms[i];
+            launches[i] = P->kt_n[i];
+        }
+    });
+}
+
+int acq_plan_reset_kernel_times(acq_plan* P) {
+    return guarded([&] {
+        if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        for (int i = 0; i < ACQ_KERNEL_KINDS; ++i) {
+            P->kt_ms[i] = 0;
+            P->kt_n[i] = 0;
+        }
+    });
+}
+
+int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t M, double* out) {
+    return guarded([&] {
+        if (!out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *out = cfar_threshold(pfa, num_cells, M);
+    });
+}
+
+int acq_gen_code(int32_t system, int32_t prn, int64_t n, double fs, double fc, double start_phase, int8_t* out) {
+    return guarded([&] {
+        if (!out && n > 0) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (n < 0) throw AcqError(ACQ_ERR_ARGUMENT, "n must be >= 0");
+        if (!(fs > 0)) throw AcqError(ACQ_ERR_ARGUMENT, "sampling frequency must be positive");
+        gen_code(system, prn, n, fs, fc, start_phase, out);
+    });
+}
+
+int acq_last_error(char* buf, size_t len) {
+    if (!buf || len == 0) return ACQ_ERR_ARGUMENT;
+    std::snprintf(buf, len, "%s", g_last_error.c_str());
+    return ACQ_OK;
+}
+
+const char* acq_version(void) { return "acqgb300 0.1.0 sm_103a"; }
+
+}  // extern "C"

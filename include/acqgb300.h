@@ -1,0 +1,195 @@
+/*
+ * acqgb300.h — C ABI of the GB300-native FM-DBZP acquisition library (libacqgb300.so).
+ *
+ * Drop-in boundary for the FM-DBZP acquisition path of JuliaGNSS/Acquisition.jl v2.6.4:
+ * a Julia `ccall` shim (or Python ctypes) maps the reference's public API onto these
+ * entry points. Plain pointers and sizes only; no CUDA or torch types cross this boundary
+ * (streams are passed as opaque `void*`).
+ *
+ * Conventions
+ *  - Every entry point returns an `int` status: ACQ_OK (0) or one of ACQ_ERR_*.
+ *    `acq_last_error` returns the message of the calling thread's last failure; for
+ *    ACQ_ERR_ARGUMENT it carries the reference's ArgumentError text.
+ *  - A plan owns all of its device memory and one CUDA stream. One acquisition per plan
+ *    at a time (the reference's contract, src/plan.jl:186-190); distinct plans may run
+ *    concurrently from different host threads.
+ *  - Indices in results are 0-based. Frequencies are in Hz, code phases in chips.
+ */
+#ifndef ACQGB300_H
+#define ACQGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define ACQ_OK 0
+#define ACQ_ERR_ARGUMENT 1          /* ArgumentError in the reference */
+#define ACQ_ERR_SHORT_SIGNAL 2      /* src/acquire.jl:68-72 */
+#define ACQ_ERR_PRN_NOT_IN_PLAN 3   /* src/acquire.jl:62-63 */
+#define ACQ_ERR_CUDA 4              /* CUDA runtime failure (message has the CUDA error) */
+#define ACQ_ERR_TIMEOUT 5           /* a bounded device wait gave up */
+#define ACQ_ERR_ALLOC 6             /* device or pinned allocation failed */
+#define ACQ_ERR_UNSUPPORTED 7
+
+/* ---- enums ---- */
+#define ACQ_GPS_L1CA 0
+#define ACQ_GPS_L5I 1
+#define ACQ_GALILEO_E1B 2            /* synthetic memory codes, BOC(1,1) */
+
+#define ACQ_CF32 0                   /* interleaved float32 re/im */
+#define ACQ_CI16 1                   /* interleaved int16 re/im */
+#define ACQ_CI8 2                    /* interleaved int8 re/im */
+#define ACQ_CF64 3                   /* interleaved float64 re/im (converted to float32 like ComplexF32(x)) */
+
+#define ACQ_NOISE_OPPOSITE_ROW 0     /* OppositeRowNoiseEstimator, src/est_signal_noise_power.jl:70 */
+#define ACQ_NOISE_GLOBAL_MEAN 1      /* GlobalMeanNoiseEstimator, src/est_signal_noise_power.jl:100 */
+
+#define ACQ_FLAG_SUBSAMPLE_INTERP 1u /* acquire!(...; subsample_interpolation = true) */
+#define ACQ_FLAG_STORE_POWER_BINS 2u /* acquire!(...; store_power_bins = true) */
+
+typedef struct acq_plan acq_plan;
+
+/* Keyword arguments of plan_acquire (src/plan.jl:312-324). */
+typedef struct {
+    int32_t system;                                  /* ACQ_GPS_L1CA, ... */
+    double sampling_freq_hz;
+    double min_doppler_coverage_hz;                  /* default 7000 */
+    int32_t num_coherently_integrated_code_periods;  /* default 1 */
+    int32_t bit_edge_search_steps;                   /* default 1 */
+    int32_t num_noncoherent_accumulations;           /* default 1 */
+    int32_t noise_estimator;                         /* default ACQ_NOISE_OPPOSITE_ROW */
+    int32_t use_secondary_code;                      /* default 1 */
+    int32_t max_secondary_code_rotations;            /* default 32 */
+    int32_t device;                                  /* CUDA device ordinal, default 0 */
+} acq_plan_desc;
+
+/* Derived plan geometry (the fields of AcquisitionPlan, src/plan.jl:81-174). */
+typedef struct {
+    int32_t samples_per_code;
+    int32_t samples_per_code_eff;
+    int32_t num_blocks;
+    int32_t block_size;
+    int32_t fft_size;
+    int32_t num_coherently_integrated_code_periods;
+    int32_t num_data_bits;
+    int32_t bit_edge_search_steps;
+    int32_t num_noncoherent_accumulations;
+    int32_t num_doppler_bins;
+    int32_t num_secondary_rotations;
+    int32_t bit_period_codes;
+    int32_t num_prns;
+    int32_t path;                 /* 0 simple, 1 data-bit / bit-edge search, 2 secondary-code rotation */
+    double doppler_first_hz;      /* doppler_freqs[0] */
+    double doppler_step_hz;       /* step(doppler_freqs) */
+    double code_length;           /* chips of the primary code */
+    double code_freq_hz;
+    double center_freq_hz;
+    double cfar_threshold_pfa001; /* cfar_threshold(0.01, cells incl. rotations; N_nc) */
+} acq_geometry;
+
+/* One AcquisitionResults (src/Acquisition.jl:81-109) plus the decision indices. */
+typedef struct {
+    int32_t prn;
+    int32_t secondary_code_phase;         /* -1 == `nothing` */
+    double carrier_doppler_hz;
+    double code_phase;                    /* chips */
+    double cn0_dbhz;
+    float noise_power;
+    float peak_to_noise_ratio;
+    float peak_power;
+    int32_t num_noncoherent_integrations;
+    int32_t peak_doppler_bin;             /* 0-based sorted Doppler row */
+    int32_t peak_code_bin;                /* 0-based effective code-phase column */
+    int32_t sign_pattern;                 /* data-bit combination at the peak, -1 on the simple path */
+    int32_t bit_edge;                     /* bit-edge alignment at the peak, -1 on the simple path */
+    int32_t detected;                     /* peak_to_noise_ratio > cfar_threshold(0.01, ...) */
+    int32_t reserved;
+} acq_result;
+
+/* Fill `desc` with the reference's keyword defaults (src/plan.jl:312-324). */
+void acq_plan_desc_init(acq_plan_desc* desc);
+
+/* Validate `desc` and derive the geometry without touching the GPU.
+ * Replaces the validation + geometry part of plan_acquire, src/plan.jl:325-525. */
+int acq_plan_query(const acq_plan_desc* desc, acq_geometry* out);
+
+/* plan_acquire(system, sampling_freq, prns; kwargs...) — src/plan.jl:312-697.
+ * `codes` may be NULL (the library samples its own codes, GNSSSignals gen_code semantics)
+ * or point to n_prns * samples_per_code int8 +-1 samples (e.g. from GNSSSignals.gen_code). */
+int acq_plan_create(const acq_plan_desc* desc, const int32_t* prns, int32_t n_prns,
+                    const int8_t* codes, acq_plan** out);
+
+int acq_plan_destroy(acq_plan* plan);
+
+int acq_plan_get_geometry(const acq_plan* plan, acq_geometry* out);
+
+/* doppler_freqs of the plan (num_doppler_bins doubles, sorted ascending). */
+int acq_plan_doppler_freqs(const acq_plan* plan, double* out);
+
+/* acquire!(plan, signal, prns; interm_freq, subsample_interpolation, store_power_bins)
+ * — src/acquire.jl:54-89. `samples` is a HOST buffer of n_samples complex samples of `dtype`.
+ * `results` receives n_prns entries in the order of `prns`. When flags has
+ * ACQ_FLAG_STORE_POWER_BINS, `power_bins` (host, may otherwise be NULL) receives
+ * n_prns * num_doppler_bins * samples_per_code_eff float32, per PRN row-major
+ * [doppler_row][code_col] (the transpose of Julia's column-major Matrix). Synchronous. */
+int acq_acquire(acq_plan* plan, const void* samples, int32_t dtype, int64_t n_samples,
+                const int32_t* prns, int32_t n_prns, double interm_freq_hz, uint32_t flags,
+                acq_result* results, float* power_bins);
+
+/* Same as acq_acquire, with `samples` already in device memory. Enqueues on the plan's
+ * stream and returns without waiting; read the results with acq_fetch_results. */
+int acq_acquire_device_async(acq_plan* plan, const void* d_samples, int32_t dtype, int64_t n_samples,
+                             const int32_t* prns, int32_t n_prns, double interm_freq_hz, uint32_t flags);
+
+/* Wait for the plan's stream and copy the last acquisition's results (and, when stored,
+ * power bins) to host memory. */
+int acq_fetch_results(acq_plan* plan, acq_result* results, float* power_bins);
+
+/* The plan's cudaStream_t, as an opaque pointer (for event timing by the caller). */
+int acq_plan_stream(const acq_plan* plan, void** stream);
+
+/* Number of this library's kernel launches enqueued by the last acquisition. */
+int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
+
+/* Kernel classes for per-launch device timing. */
+#define ACQ_KERNEL_FRONTEND 0        /* downconversion + double-block FFT */
+#define ACQ_KERNEL_TILE 1            /* code-spectrum multiply + inverse FFT (coherent tile) */
+#define ACQ_KERNEL_COLUMN 2          /* Doppler column stage (simple / sign / rotation search) */
+#define ACQ_KERNEL_STATS 3           /* peak + FP64 noise partial sums */
+#define ACQ_KERNEL_EXTRACT 4         /* result extraction, CFAR gate, interpolation */
+#define ACQ_KERNEL_SECONDARY 5       /* secondary-code despread */
+#define ACQ_KERNEL_KINDS 8
+
+/* Enable (1) or disable (0) CUDA-event timing of every launch of this plan (on the plan's
+ * stream). Diagnostic only; no reference counterpart. */
+int acq_plan_set_kernel_timing(acq_plan* plan, int32_t enable);
+
+/* Accumulated device milliseconds and launch counts per kernel class since the last reset
+ * (arrays of n_kinds <= ACQ_KERNEL_KINDS entries). Call after acq_fetch_results. */
+int acq_plan_kernel_times(acq_plan* plan, double* total_ms, int64_t* launches, int32_t n_kinds);
+
+int acq_plan_reset_kernel_times(acq_plan* plan);
+
+/* cfar_threshold(pfa, num_cells; num_noncoherent_integrations) — src/cfar.jl:64-85. Host only. */
+int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_integrations, double* out);
+
+/* gen_code(n, system, prn, sampling_freq, code_freq, start_phase) into `out` (+-1 int8).
+ * code_freq_hz <= 0 selects the system's nominal code rate. Host only. */
+int acq_gen_code(int32_t system, int32_t prn, int64_t n, double sampling_freq_hz, double code_freq_hz,
+                 double start_phase, int8_t* out);
+
+/* Copy the calling thread's last error message (NUL-terminated, truncated to len). */
+int acq_last_error(char* buf, size_t len);
+
+/* Library version string, e.g. "acqgb300 0.1.0 sm_103a". */
+const char* acq_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACQGB300_H */

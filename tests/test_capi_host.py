@@ -1,0 +1,144 @@
+"""CPU tests of libacqgb300's host side through its C ABI (no GPU needed).
+
+The library must load here, export every symbol include/acqgb300.h declares, and agree with
+the oracle on geometry, validation, code generation and the CFAR threshold.
+"""
+import ctypes as C
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+import acqgb300 as A
+from acqgb300 import _lib as L
+from oracle import acq_oracle as O
+from oracle import gnss_codes as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SYS = {"GPSL1CA": (A.GPSL1CA(), G.GPSL1CA), "GPSL5I": (A.GPSL5I(), G.GPSL5I),
+       "GalileoE1B": (A.GalileoE1B(), G.GalileoE1B)}
+
+
+def test_library_exports_every_header_symbol():
+    header = open(os.path.join(ROOT, "include", "acqgb300.h")).read()
+    declared = set(re.findall(r"\b(acq_[a-z_0-9]+)\s*\(", header))
+    assert declared, "no declarations parsed"
+    lib = C.CDLL(L.LIB_PATH)
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(L.EXPORTED) == declared
+    assert b"sm_103a" in L.load().acq_version()
+
+
+def test_result_struct_layout():
+    assert C.sizeof(L.Result) == 72
+    assert C.sizeof(L.PlanDesc) == 56
+
+
+CONFIGS = [
+    ("GPSL1CA", 4e6, 7000, 1, 1, 1), ("GPSL1CA", 5e6, 5000, 10, 1, 8), ("GPSL1CA", 5e6, 5000, 40, 1, 2),
+    ("GPSL1CA", 5e6, 5000, 40, 4, 2), ("GPSL1CA", 5e6, 5000, 10, 2, 8), ("GPSL1CA", 2.048e6, 10000, 40, 4, 5),
+    ("GPSL1CA", 16.368e6, 5000, 5, 1, 1), ("GPSL1CA", 16.368e6, 5000, 3, 3, 1), ("GPSL1CA", 10e6, 7000, 20, 1, 1),
+    ("GPSL1CA", 1.542e6, 7000, 1, 1, 1), ("GPSL5I", 20e6, 10000, 20, 1, 4), ("GPSL5I", 20e6, 10000, 20, 2, 4),
+    ("GPSL5I", 25e6, 8000, 10, 1, 1), ("GPSL5I", 10.24e6, 1000, 10, 1, 1), ("GPSL5I", 12e6, 7000, 1, 1, 3),
+    ("GalileoE1B", 12e6, 8000, 1, 1, 1), ("GalileoE1B", 12e6, 8000, 1, 1, 5),
+]
+
+
+@pytest.mark.parametrize("cfg", CONFIGS, ids=lambda c: "-".join(map(str, c)))
+def test_geometry_matches_oracle(cfg):
+    name, fs, cov, n_coh, n_be, n_nc = cfg
+    a_sys, o_sys = SYS[name]
+    g = A.plan_geometry(a_sys, fs, min_doppler_coverage=cov, num_coherently_integrated_code_periods=n_coh,
+                        bit_edge_search_steps=n_be, num_noncoherent_accumulations=n_nc)
+    o = O.plan_geometry(o_sys, fs, cov, n_coh, n_be, n_nc)
+    assert (g.samples_per_code, g.samples_per_code_eff, g.num_blocks, g.block_size, g.fft_size, g.num_data_bits,
+            g.num_doppler_bins, g.num_secondary_rotations) == (o["spc"], o["spc_eff"], o["nb"], o["bs"], o["F"],
+                                                               o["ndb"], o["ndop"], o["R"])
+    assert g.doppler_first_hz == o["freqs"][0] and g.doppler_step_hz == o["step"]
+    thr = O.cfar_threshold(0.01, o["ndop"] * o["spc"] * o["R"], n_nc)
+    assert g.cfar_threshold_pfa001 == pytest.approx(thr, rel=1e-10)
+
+
+BAD = [dict(num_coherently_integrated_code_periods=30), dict(num_coherently_integrated_code_periods=20,
+       bit_edge_search_steps=3), dict(bit_edge_search_steps=2), dict(num_noncoherent_accumulations=0),
+       dict(num_coherently_integrated_code_periods=0), dict(bit_edge_search_steps=0),
+       dict(min_doppler_coverage=1.1e6)]
+
+
+@pytest.mark.parametrize("kw", BAD)
+def test_validation_errors_match_oracle(kw):
+    with pytest.raises(A.ArgumentError):
+        A.plan_geometry(A.GPSL1CA(), 2.048e6, **kw)
+    okw = dict(min_doppler_coverage=kw.get("min_doppler_coverage", 7000.0),
+               n_coh=kw.get("num_coherently_integrated_code_periods", 1), n_be=kw.get("bit_edge_search_steps", 1),
+               n_nc=kw.get("num_noncoherent_accumulations", 1))
+    with pytest.raises(O.ArgumentError):
+        O.plan_geometry(G.GPSL1CA, 2.048e6, **okw)
+
+
+def test_secondary_code_error_messages():
+    # test/plan.jl:70-121 text checks
+    with pytest.raises(A.ArgumentError) as e:
+        A.plan_geometry(A.GPSL5I(), 10.24e6, min_doppler_coverage=1000, num_coherently_integrated_code_periods=5)
+    m = str(e.value)
+    for s in ("secondary", "5", "10", "68", "num_coherently_integrated_code_periods",
+              "num_noncoherent_accumulations", "use_secondary_code"):
+        assert s in m
+    with pytest.raises(A.ArgumentError) as e:
+        A.plan_geometry(A.GPSL5I(), 10.24e6, min_doppler_coverage=1000, num_coherently_integrated_code_periods=10,
+                        max_secondary_code_rotations=8)
+    assert "max_secondary_code_rotations" in str(e.value) and "GPSL5I" in str(e.value)
+    g = A.plan_geometry(A.GPSL5I(), 10.24e6, min_doppler_coverage=1000, num_coherently_integrated_code_periods=5,
+                        use_secondary_code=False)
+    assert g.num_secondary_rotations == 1
+
+
+@pytest.mark.parametrize("name,fs,fc_off,start", [
+    ("GPSL1CA", 4e6, 0.0, 0.0), ("GPSL1CA", 5e6, 0.0, 300.5), ("GPSL1CA", 10e6, 0.81, 123.456),
+    ("GPSL5I", 10.24e6, 0.0, 0.0), ("GPSL5I", 20e6, 7.8, 5115.3), ("GPSL5I", 25e6, 0.0, 0.0),
+    ("GalileoE1B", 12e6, 0.0, 0.0), ("GalileoE1B", 12e6, 1.1, 2000.25)])
+def test_gen_code_matches_oracle(name, fs, fc_off, start):
+    a_sys, o_sys = SYS[name]
+    n = 3 * int(math.ceil(o_sys.code_length / o_sys.code_freq * fs))
+    for prn in (1, 7, 32):
+        fc = o_sys.code_freq + fc_off
+        a = a_sys.gen_code(n, prn, fs, fc, start)
+        o = G.gen_code(n, o_sys, prn, fs, fc, start)
+        assert np.array_equal(a, o), (name, prn)
+
+
+def test_gen_code_l5i_all_prns_and_l1_all_prns():
+    for prn in range(1, 38):
+        assert np.array_equal(A.GPSL5I().gen_code(10230, prn, 10.23e6), G.GPSL5I.full_chips(prn)[:10230])
+    for prn in range(1, 33):
+        assert np.array_equal(A.GPSL1CA().gen_code(1023, prn, 1.023e6), G.l1ca_chips(prn))
+
+
+@pytest.mark.parametrize("M", [1, 2, 3, 4, 8, 16])
+def test_cfar_threshold_matches_scipy(M):
+    for pfa in (0.1, 0.01, 1e-3):
+        for cells in (1, 100, 10_000, 1_000_000, 100_000_000, 2_000_000_000):
+            assert A.cfar_threshold(pfa, cells, M) == pytest.approx(O.cfar_threshold(pfa, cells, M), rel=1e-9)
+    assert A.cfar_threshold(0.01, 1) == pytest.approx(-math.log(0.01), rel=1e-12)
+
+
+def test_cfar_argument_errors():
+    for bad in [(0.0, 100), (1.0, 100), (-0.1, 100), (0.01, 0)]:
+        with pytest.raises(A.ArgumentError):
+            A.cfar_threshold(*bad)
+    with pytest.raises(A.ArgumentError):
+        A.cfar_threshold(0.01, 100, 0)
+
+
+def test_plan_create_fails_loudly_without_gpu():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(A.AcquisitionError):
+        A.plan_acquire(A.GPSL1CA(), 4e6, [1])

@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on seeded inputs.
+
+Bars (written here, checked per case):
+* decisions bit-exact: detected set, peak Doppler row, peak code-phase column, sign pattern,
+  bit edge, secondary-code phase; compared with the FP64 oracle, and skipped for a PRN only
+  when the FP32 and FP64 oracles themselves disagree (a near-tie both implementations may
+  break either way; counted and printed).
+* power surface: |P_gpu - P_64| <= POWER_RTOL * max(P_64) for every cell (relative to the
+  surface peak), and the error against the FP64 oracle is printed next to the FP32 oracle's.
+* noise power, peak-to-noise ratio, code phase and Doppler: within 1e-4 relative.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import acqgb300 as A
+from acqgb300 import synth
+from oracle import acq_oracle as O
+from oracle import gnss_codes as G
+
+pytestmark = pytest.mark.gpu
+
+POWER_RTOL = 1e-4
+SCALAR_RTOL = 1e-4
+
+SYS = {"GPSL1CA": (A.GPSL1CA, G.GPSL1CA), "GPSL5I": (A.GPSL5I, G.GPSL5I), "GalileoE1B": (A.GalileoE1B, G.GalileoE1B)}
+
+
+def _run_case(name, fs, prns, n_coh=1, n_be=1, n_nc=1, cov=7000.0, sats=(), seed=1, interm_freq=0.0,
+              quant=None, interp=False, noise_estimator="opposite_row", use_secondary_code=True):
+    a_sys, o_sys = SYS[name]
+    a_sys = a_sys()
+    plan = A.plan_acquire(a_sys, fs, prns, min_doppler_coverage=cov, num_coherently_integrated_code_periods=n_coh,
+                          bit_edge_search_steps=n_be, num_noncoherent_accumulations=n_nc,
+                          noise_estimator=(A.GlobalMeanNoiseEstimator() if noise_estimator == "global_mean"
+                                           else A.OppositeRowNoiseEstimator()),
+                          use_secondary_code=use_secondary_code)
+    n = n_nc * n_coh * plan.samples_per_code
+    x = synth.synth(a_sys, fs, n, list(sats), seed, interm_freq=interm_freq)
+    if quant == "ci16":
+        sig = synth.to_ci16(x)
+        osig = (sig[:, 0].astype(np.float32) + 1j * sig[:, 1].astype(np.float32)).astype(np.complex64)
+    elif quant == "ci8":
+        sig = synth.to_ci8_3bit(x)
+        osig = (sig[:, 0].astype(np.float32) + 1j * sig[:, 1].astype(np.float32)).astype(np.complex64)
+    else:
+        sig = x.astype(np.complex64)
+        osig = sig
+    res = A.acquire_b(plan, sig, prns, interm_freq=interm_freq, subsample_interpolation=interp,
+                      store_power_bins=True)
+    outs = {}
+    for prec in ("f32", "f64"):
+        op = O.plan_acquire(o_sys, fs, prns, min_doppler_coverage=cov, num_coherently_integrated_code_periods=n_coh,
+                            bit_edge_search_steps=n_be, num_noncoherent_accumulations=n_nc,
+                            noise_estimator=noise_estimator, use_secondary_code=use_secondary_code, precision=prec)
+        outs[prec] = O.acquire_b(op, osig, prns, interm_freq=interm_freq, subsample_interpolation=interp,
+                                 return_surfaces=True)
+    return plan, res, outs
+
+
+def _compare(res, outs, label):
+    r32, s32 = outs["f32"]
+    r64, s64 = outs["f64"]
+    ties = 0
+    worst_gpu = worst_o32 = 0.0
+    for g, a, b, sa, sb in zip(res, r32, r64, s32, s64):
+        P64 = sb.power
+        scale = float(P64.max())
+        err_gpu = float(np.abs(g.power_bins.astype(np.float64) - P64).max()) / scale
+        err_o32 = float(np.abs(sa.power.astype(np.float64) - P64).max()) / scale
+        worst_gpu, worst_o32 = max(worst_gpu, err_gpu), max(worst_o32, err_o32)
+        assert err_gpu <= POWER_RTOL, (label, g.prn, err_gpu)
+        if (a.peak_doppler_bin, a.peak_code_bin) != (b.peak_doppler_bin, b.peak_code_bin):
+            ties += 1
+            continue
+        assert (g.peak_doppler_bin, g.peak_code_bin) == (b.peak_doppler_bin, b.peak_code_bin), (label, g.prn)
+        assert g.sign_pattern == b.sign_pattern and g.bit_edge == b.bit_edge, (label, g.prn)
+        assert A.is_detected(g) == O.is_detected(b), (label, g.prn)
+        assert g.secondary_code_phase == b.secondary_code_phase, (label, g.prn)
+        assert float(g.noise_power) == pytest.approx(b.noise_power, rel=SCALAR_RTOL)
+        assert float(g.peak_to_noise_ratio) == pytest.approx(b.peak_to_noise_ratio, rel=SCALAR_RTOL)
+        assert g.code_phase == pytest.approx(b.code_phase, rel=SCALAR_RTOL, abs=1e-6)
+        assert g.carrier_doppler == pytest.approx(b.carrier_doppler, rel=SCALAR_RTOL, abs=1e-3)
+        assert g.CN0 == pytest.approx(b.CN0, rel=SCALAR_RTOL)
+    print(f"[{label}] max |P_gpu-P64|/max = {worst_gpu:.3e}  (FP32 oracle {worst_o32:.3e}); near-ties {ties}")
+    return ties
+
+
+def test_cfg1_l1ca_4mhz_32prns():
+    sats = [synth.Satellite(1, 45.0, 1234.0, 300.5)]
+    plan, res, outs = _run_case("GPSL1CA", 4e6, list(range(1, 33)), sats=sats, seed=11)
+    assert plan.num_doppler_bins == 16 and plan.num_blocks == 16
+    _compare(res, outs, "cfg1")
+    assert A.is_detected(res[0]) and abs(res[0].code_phase - 300.5) < 1.0
+
+
+def test_l1ca_multistep_drift_ci16():
+    rng = np.random.default_rng(5)
+    sats = synth.random_sats(rng, [3, 9], (42, 45), 5000, 1023, 0.02)
+    plan, res, outs = _run_case("GPSL1CA", 5e6, [3, 9, 17], n_coh=10, n_nc=4, cov=5000, sats=sats, seed=5,
+                                quant="ci16")
+    assert plan.num_doppler_bins == 200
+    _compare(res, outs, "l1-10msx4-ci16")
+
+
+def test_l1ca_interm_freq_interp_global_mean():
+    sats = [synth.Satellite(5, 47.0, 500.0, 150.3), synth.Satellite(6, 44.0, -2600.0, 800.7)]
+    for est in ("opposite_row", "global_mean"):
+        plan, res, outs = _run_case("GPSL1CA", 2.048e6, [5, 6, 7], sats=sats, seed=3333, interm_freq=1000.0,
+                                    interp=True, noise_estimator=est)
+        _compare(res, outs, f"l1-if-interp-{est}")
+
+
+def test_sign_search_two_bits_bit_edge():
+    sats = [synth.Satellite(1, 45.0, 1500.0, 100.0, bit_offset=0.013)]
+    plan, res, outs = _run_case("GPSL1CA", 2.048e6, [1, 2], n_coh=40, n_be=4, cov=5000, sats=sats, seed=21)
+    assert plan.num_data_bits == 2
+    _compare(res, outs, "sign-ndb2-nbe4")
+
+
+def test_sign_search_odd_doppler_bins_quirk():
+    sats = [synth.Satellite(2, 48.0, 700.0, 512.25)]
+    plan, res, outs = _run_case("GPSL1CA", 16.368e6, [2], n_coh=3, n_be=3, cov=5000, sats=sats, seed=8)
+    assert plan.num_doppler_bins % 2 == 1
+    _compare(res, outs, "sign-odd-ndop")
+
+
+def test_rotation_l5i_nh10_every_phase():
+    fs = 10.24e6
+    a_sys = A.GPSL5I()
+    primary = a_sys.gen_code(10240, 1, fs).astype(np.complex64)
+    plan = A.plan_acquire(a_sys, fs, [1], min_doppler_coverage=1000, num_coherently_integrated_code_periods=10)
+    for r in range(10):
+        sig = np.concatenate([np.float32(G.NH10[(k + r) % 10]) * primary for k in range(10)])
+        res = A.acquire_b(plan, sig, [1])[0]
+        assert res.secondary_code_phase == r
+
+
+def test_rotation_l5i_data_bits_multistep():
+    rng = np.random.default_rng(2)
+    sats = [synth.Satellite(1, 46.0, 900.0, 1234.5), synth.Satellite(4, 44.0, -3100.0, 6000.0)]
+    plan, res, outs = _run_case("GPSL5I", 12e6, [1, 4, 5], n_coh=20, n_nc=2, cov=5000, sats=sats, seed=2,
+                                interp=True)
+    assert plan.num_secondary_rotations == 10 and plan.num_data_bits == 2
+    _compare(res, outs, "rot-l5i-20msx2")
+
+
+def test_rotation_l5i_streamed_ci8():
+    sats = [synth.Satellite(2, 50.0, -1700.0, 333.3)]
+    plan, res, outs = _run_case("GPSL5I", 10.24e6, [2, 3], n_coh=10, cov=5000, sats=sats, seed=4, quant="ci8")
+    _compare(res, outs, "rot-l5i-10ms-ci8")
+
+
+def test_e1b_boc_12mhz():
+    sats = [synth.Satellite(11, 48.0, 2500.0, 2000.25, data_bits=False)]
+    plan, res, outs = _run_case("GalileoE1B", 12e6, [11, 12], cov=8000, sats=sats, seed=9)
+    _compare(res, outs, "e1b-12mhz")
+
+
+def test_opt_out_golden_vector_on_gpu():
+    # test/secondary_code_search.jl:119-130 through the CUDA path
+    fs = 10.24e6
+    a_sys = A.GPSL5I()
+    primary = a_sys.gen_code(10240, 1, fs).astype(np.complex64)
+    sig = np.concatenate([np.float32(G.NH10[k]) * primary for k in range(10)])
+    plan = A.plan_acquire(a_sys, fs, [1], min_doppler_coverage=1000, num_coherently_integrated_code_periods=10,
+                          use_secondary_code=False)
+    nim = A.acquire_b(plan, sig, [1], store_power_bins=True)[0].power_bins
+    assert nim.shape == (40, 10240)
+    assert nim.max() == pytest.approx(1.146687232e9, rel=1e-4)
+    assert nim.astype(np.float64).sum() == pytest.approx(5.2553412608e10, rel=1e-4)
+    assert nim[0, 99] == pytest.approx(8.2944015625e4, rel=1e-4)
+    assert nim[-1, -1] == pytest.approx(2.318815625e4, rel=1e-4)
+
+
+def test_argument_errors_through_cabi():
+    plan = A.plan_acquire(A.GPSL1CA(), 2.048e6, [1, 2])
+    with pytest.raises(A.ArgumentError, match="avail_prns"):
+        A.acquire_b(plan, np.zeros(2048, np.complex64), [3])
+    with pytest.raises(A.ArgumentError, match="Provide a longer signal"):
+        A.acquire_b(plan, np.zeros(100, np.complex64), [1])
+
+
+def test_power_bins_cached_buffer_reused():
+    # test/plan.jl:329-356 reuse contract
+    plan = A.plan_acquire(A.GPSL1CA(), 2.048e6, [1, 2])
+    sig = synth.synth(A.GPSL1CA(), 2.048e6, 2048, [synth.Satellite(1, 45, 0.0, 10.0)], 1).astype(np.complex64)
+    assert all(b is None for b in plan.result_buffers)
+    A.acquire_b(plan, sig, [1, 2])
+    assert all(b is None for b in plan.result_buffers)
+    r = A.acquire_b(plan, sig, [1, 2], store_power_bins=True)
+    assert r[0].power_bins is plan.result_buffers[0]
+    cached = plan.result_buffers[0]
+    r2 = A.acquire_b(plan, sig, [1, 2], store_power_bins=True)
+    assert plan.result_buffers[0] is cached and np.array_equal(r2[0].power_bins, cached)
