@@ -157,6 +157,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--accumulations", type=int, default=N_NC,
+                    help="non-coherent accumulations (profiling cases only; the workload uses 8)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -179,8 +181,9 @@ def main():
         dist.init_process_group("nccl")
 
     ci16, sats = make_input()
+    n_nc = args.accumulations
     plan = A.plan_acquire(A.GPSL1CA(), FS, PRNS, min_doppler_coverage=COV, num_coherently_integrated_code_periods=N_COH,
-                          num_noncoherent_accumulations=N_NC, device=local_rank)
+                          num_noncoherent_accumulations=n_nc, device=local_rank)
     host = torch.from_numpy(ci16).pin_memory()
     dev = host.to(f"cuda:{local_rank}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
@@ -266,7 +269,7 @@ def main():
     alg_bytes = {
         "tile": n_prn * ndop * spc * 8 + ndop * F * 8 + n_prn * nb * F * 8,        # T write + S, C* reads
         "column": n_prn * ndop * spc * 8 + n_prn * ndop * spc * 4 * 2,              # T read + acc read/write
-        "frontend": N_NC * N_COH * spc * 4 + N_NC * ndop * F * 8,
+        "frontend": n_nc * N_COH * spc * 4 + n_nc * ndop * F * 8,
         "stats": n_prn * ndop * spc * 4,
     }
     ab = alg_bytes.get(name)
@@ -284,12 +287,12 @@ def main():
         cpu = {"value": 1.0 / per_acq, "unit": "acq/s", "cores": os.cpu_count(), "kind": "port",
                "sample": "oracle FP32 numpy/scipy restatement, 1 PRN x 8 accumulation steps, x32 PRNs "
                          "(scipy.fft workers=-1)"}
-    samples = N_NC * N_COH * spc
+    samples = n_nc * N_COH * spc
     det = [r.prn for r in res if A.is_detected(r)]
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, CI16)",
-            "config": {"workload": WORKLOAD, "prns": n_prn, "samples": samples, "num_doppler_bins": ndop,
+            "config": {"workload": WORKLOAD if n_nc == N_NC else f"{WORKLOAD}_nnc{n_nc}", "prns": n_prn, "samples": samples, "num_doppler_bins": ndop,
                        "samples_per_code": spc, "fft_size": F, "form": "plain",
                        "l2": "flushed (256 MB write) before every timed step"},
             "msample_prn_per_s": value * n_prn * samples / 1e6,
