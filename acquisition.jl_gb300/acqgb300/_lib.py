@@ -44,6 +44,11 @@ class Geometry(C.Structure):
         "cfar_threshold_pfa001")]
 
 
+class NoiseStats(C.Structure):
+    _fields_ = [("signal_power", C.c_float), ("noise_power", C.c_float), ("peak_power", C.c_float),
+                ("peak_doppler_bin", C.c_int32), ("peak_code_bin", C.c_int32), ("reserved", C.c_int32)]
+
+
 class Result(C.Structure):
     _fields_ = [("prn", C.c_int32), ("secondary_code_phase", C.c_int32), ("carrier_doppler_hz", C.c_double),
                 ("code_phase", C.c_double), ("cn0_dbhz", C.c_double), ("noise_power", C.c_float),
@@ -57,7 +62,7 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_plan_doppler_freqs", "acq_acquire", "acq_acquire_device_async", "acq_fetch_results",
             "acq_plan_stream", "acq_plan_last_launch_count", "acq_cfar_threshold", "acq_gen_code",
             "acq_last_error", "acq_version", "acq_plan_set_kernel_timing", "acq_plan_kernel_times",
-            "acq_plan_reset_kernel_times"]
+            "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc"]
 KERNEL_KINDS = 8
 KERNEL_NAMES = ["frontend", "tile", "column", "stats", "extract", "secondary", "k6", "k7"]
 
@@ -96,6 +101,8 @@ def load():
     lib.acq_plan_set_kernel_timing.argtypes = [P, C.c_int32]
     lib.acq_plan_kernel_times.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int32]
     lib.acq_plan_reset_kernel_times.argtypes = [P]
+    lib.acq_est_signal_noise_power_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_double,
+                                                       C.c_int32, C.c_void_p, C.c_void_p]
     lib.acq_version.restype = C.c_char_p
     for name in EXPORTED:
         if name not in ("acq_plan_desc_init", "acq_version"):

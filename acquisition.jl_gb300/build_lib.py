@@ -44,15 +44,18 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
     opt = ["-O0", "-g"] if debug else ["-O3"]
     host_obj = os.path.join(BUILD_DIR, "acq_host.o")
     dev_obj = os.path.join(BUILD_DIR, "acq_runtime.o")
+    na_obj = os.path.join(BUILD_DIR, "acq_noalloc.o")
     host_cmd = ["g++", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", *opt,
                 f"-I{INCLUDE}", "-c", os.path.join(CSRC, "acq_host.cpp"), "-o", host_obj]
     dev_cmd = [nvcc, "-std=c++17", *ARCH, "-lineinfo", *opt, "-Xcompiler", "-fPIC,-ffp-contract=off",
                f"-I{INCLUDE}", f"-I{CSRC}", "-c", os.path.join(CSRC, "acq_runtime.cu"), "-o", dev_obj]
+    na_cmd = [nvcc, "-std=c++17", *ARCH, "-lineinfo", *opt, "-Xcompiler", "-fPIC,-ffp-contract=off",
+              f"-I{INCLUDE}", f"-I{CSRC}", "-c", os.path.join(CSRC, "acq_noalloc.cu"), "-o", na_obj]
     if ptxas_verbose:
         dev_cmd.insert(1, "-Xptxas=-v")
-    with ThreadPoolExecutor(2) as ex:
-        outs = list(ex.map(_run, [host_cmd, dev_cmd]))
-    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, "-o", LIB + ".tmp", "-lcudart_static", "-lrt", "-ldl",
+    with ThreadPoolExecutor(3) as ex:
+        outs = list(ex.map(_run, [host_cmd, dev_cmd, na_cmd]))
+    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, na_obj, "-o", LIB + ".tmp", "-lcudart_static", "-lrt", "-ldl",
                 "-lpthread"]
     outs.append(_run(link_cmd))
     os.replace(LIB + ".tmp", LIB)

@@ -63,6 +63,9 @@ double cfar_threshold(double pfa, int64_t num_cells, int M);   // src/cfar.jl:64
 
 int nextprod_2357(int n);
 
+// Record the calling thread's last error message (read back by acq_last_error).
+void set_last_error(const std::string& msg);
+
 // FFT factorisation used by the device Stockham FFT (radices 4,2,3,5,7, then odd primes).
 std::vector<int> fft_radices(int n);
 

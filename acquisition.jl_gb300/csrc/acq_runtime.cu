@@ -438,6 +438,8 @@ void fill_geometry(const Geometry& g, const SystemInfo& s, int n_prns, acq_geome
 
 }  // namespace
 
+void acq::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 extern "C" {
 
 void acq_plan_desc_init(acq_plan_desc* d) {

@@ -182,6 +182,33 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_in
 int acq_gen_code(int32_t system, int32_t prn, int64_t n, double sampling_freq_hz, double code_freq_hz,
                  double start_phase, int8_t* out);
 
+/* Output of acq_est_signal_noise_power_noalloc (device memory owned by the caller). */
+typedef struct {
+    float signal_power;        /* peak_power - noise_power */
+    float noise_power;
+    float peak_power;
+    int32_t peak_doppler_bin;  /* 0-based row */
+    int32_t peak_code_bin;     /* 0-based column */
+    int32_t reserved;
+} acq_noise_stats;
+
+/* Peak and noise power of a power surface, for callers that cannot allocate device memory
+ * once running (a receiver's real-time processing thread, where cudaMalloc/cudaFree may
+ * synchronise the device and take unbounded time, or a plugin whose host framework owns all
+ * device memory). This entry point has no counterpart in the reference; it computes what
+ * acq_acquire reports for a surface (peak with the lowest-column, lowest-row tie-break,
+ * OppositeRow or GlobalMean noise in FP64) and allocates nothing: `d_power_bins`
+ * (num_doppler_bins rows x num_code_bins columns, row-major float32) and `d_out` are caller
+ * device memory; the scratch is a fixed static device array (32 KiB, held by every GPU that
+ * loads the library until exit), so num_doppler_bins is limited to 4096 and larger sizes
+ * return ACQ_ERR_ARGUMENT. Asynchronous on `stream` (a cudaStream_t, NULL for the default
+ * stream). Calls share the scratch and clear it themselves; calls that overlap on the GPU race
+ * and must be ordered by the caller. The first call on a device resolves the scratch address
+ * (cudaGetSymbolAddress); make it before any stream capture. */
+int acq_est_signal_noise_power_noalloc(const float* d_power_bins, int32_t num_doppler_bins, int64_t num_code_bins,
+                                       double sampling_freq_hz, double code_freq_hz, int32_t noise_estimator,
+                                       acq_noise_stats* d_out, void* stream);
+
 /* Copy the calling thread's last error message (NUL-terminated, truncated to len). */
 int acq_last_error(char* buf, size_t len);
 

@@ -1,0 +1,70 @@
+"""The no-allocation statistics entry point against acq_acquire, through the C ABI.
+
+acq_est_signal_noise_power_noalloc serves callers that cannot allocate device memory while
+running (a receiver's real-time processing thread, where cudaMalloc/cudaFree may synchronise
+the device and stall it, or a plugin whose host framework owns all device memory). Given the
+power surface that acq_acquire stored, it must report the same peak cell and, within the
+tolerance of the parity tests, the same noise power, on consecutive calls that share its
+static scratch. This file is collected last on purpose.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import acqgb300 as A
+from acqgb300 import _lib as L
+from acqgb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4   # SCALAR_RTOL of tests/test_gpu_parity.py
+
+
+def _noalloc(power_bins: np.ndarray, fs: float, fc: float, estimator: int) -> L.NoiseStats:
+    import torch
+    surf = torch.from_numpy(np.ascontiguousarray(power_bins, dtype=np.float32)).cuda()
+    out = torch.zeros(C.sizeof(L.NoiseStats), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    st = L.load().acq_est_signal_noise_power_noalloc(C.c_void_p(surf.data_ptr()), surf.shape[0], surf.shape[1],
+                                                     fs, fc, estimator, C.c_void_p(out.data_ptr()), None)
+    assert st == L.ACQ_OK, L.last_error()
+    torch.cuda.synchronize()
+    return L.NoiseStats.from_buffer_copy(out.cpu().numpy().tobytes())
+
+
+def _acquired(estimator):
+    fs = 5e6
+    sats = [synth.Satellite(3, 44.0, 2300.0, 411.7), synth.Satellite(9, 41.0, -1800.0, 77.2)]
+    plan = A.plan_acquire(A.GPSL1CA(), fs, [3, 9, 12], min_doppler_coverage=5000,
+                          num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=2,
+                          noise_estimator=estimator)
+    x = synth.synth(A.GPSL1CA(), fs, 2 * 10 * plan.samples_per_code, sats, seed=31).astype(np.complex64)
+    return A.acquire_b(plan, x, [3, 9, 12], store_power_bins=True), fs
+
+
+def _check(stats: L.NoiseStats, r):
+    assert (stats.peak_doppler_bin, stats.peak_code_bin) == (r.peak_doppler_bin, r.peak_code_bin)
+    assert stats.peak_power == float(r.peak_power)
+    assert stats.noise_power == pytest.approx(float(r.noise_power), rel=RTOL)
+    assert stats.signal_power == pytest.approx(float(r.peak_power) - float(r.noise_power), rel=RTOL)
+
+
+def test_noalloc_matches_acquire_on_consecutive_calls():
+    fc = A.GPSL1CA().code_frequency
+    res_or, fs = _acquired(A.OppositeRowNoiseEstimator())
+    res_gm, _ = _acquired(A.GlobalMeanNoiseEstimator())
+    # several calls in a row share (and re-clear) the static scratch
+    for r, est in [(res_or[0], L.ACQ_NOISE_OPPOSITE_ROW), (res_gm[1], L.ACQ_NOISE_GLOBAL_MEAN),
+                   (res_or[2], L.ACQ_NOISE_OPPOSITE_ROW), (res_gm[0], L.ACQ_NOISE_GLOBAL_MEAN)]:
+        _check(_noalloc(r.power_bins, fs, fc, est), r)
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch():
+    import torch
+    dummy = torch.zeros(16, dtype=torch.float32, device="cuda")
+    out = torch.zeros(C.sizeof(L.NoiseStats), dtype=torch.uint8, device="cuda")
+    st = L.load().acq_est_signal_noise_power_noalloc(C.c_void_p(dummy.data_ptr()), 5000, 100, 5e6, 1.023e6,
+                                                     L.ACQ_NOISE_OPPOSITE_ROW, C.c_void_p(out.data_ptr()), None)
+    assert st == L.ACQ_ERR_ARGUMENT
+    assert "4096" in L.last_error()
