@@ -11,6 +11,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 namespace acq {
 
 constexpr int kMaxFftStages = 24;
@@ -158,6 +160,128 @@ __device__ void fft_block(float2*& src, float2*& dst, const FftDesc& d, int B, i
         src = dst;
         dst = t;
     }
+}
+
+
+// ======================================================================================
+// Register FFTs and the two-pass (four-step) shared-memory FFT for hot sizes.
+//
+// RegFFT<N> runs an N-point DFT on N values held in registers, fully unrolled: split
+// N = P * M with P the first of 4, 2, 3, 5, 7 dividing N; P-point DFTs on the strided
+// elements, twiddles W_N^{m k} from constant memory at compile-time indices, then M-point
+// DFTs recursively on contiguous sub-blocks. The output is in a compile-time permutation
+// (reg_perm<N>(f) is the register holding X[f]).
+//
+// FourStep<N1, N2>: N = N1 * N2 points in shared memory. Pass 1 (one task per n2): DFT_N1 over
+// x[n2 + N2 n1], multiply by W_N^{n2 k1}, store in place. Pass 2 (one task per k1): DFT_N2 over
+// the contiguous y[N2 k1 + n2] gives X[k1 + N1 k2].
+// ======================================================================================
+
+constexpr int kRegTwMax = 64;  // register-FFT sizes 2..64 have constant twiddle tables
+__host__ __device__ constexpr int reg_tw_offset(int n) { return (n - 1) * n / 2 - 1; }  // sum_{k=2}^{n-1} k
+constexpr int kRegTwEntries = reg_tw_offset(kRegTwMax + 1);
+__constant__ float2 c_regtw[kRegTwEntries];  // W_n^e = exp(-2 pi i e / n), filled by the host
+
+__host__ __device__ constexpr int first_factor(int n) {
+    return n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : n % 7 == 0 ? 7 : n;
+}
+
+__host__ __device__ constexpr int reg_perm(int n, int f) {
+    // register index holding X[f] after RegFFT<n>
+    return (first_factor(n) == n) ? f
+                                  : (f % first_factor(n)) * (n / first_factor(n)) +
+                                        reg_perm(n / first_factor(n), f / first_factor(n));
+}
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I in [B, E).
+template <int B, int E, typename Fn>
+__device__ __forceinline__ void static_for(Fn&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
+template <int P, bool INV>
+__device__ __forceinline__ void base_dft(float2* v) {
+    if constexpr (P == 2) bf2<INV>(v);
+    else if constexpr (P == 3) bf3<INV>(v);
+    else if constexpr (P == 4) bf4<INV>(v);
+    else if constexpr (P == 5) bf5<INV>(v);
+    else {
+        float2 o[P];
+#pragma unroll
+        for (int t = 0; t < P; ++t) {
+            float2 acc = v[0];
+#pragma unroll
+            for (int q = 1; q < P; ++q) {
+                float2 w = c_regtw[reg_tw_offset(P) + (q * t) % P];
+                if (INV) w.y = -w.y;
+                acc = c_add(acc, c_mul(v[q], w));
+            }
+            o[t] = acc;
+        }
+#pragma unroll
+        for (int t = 0; t < P; ++t) v[t] = o[t];
+    }
+}
+
+template <int N, bool INV>
+struct RegFFT {
+    static constexpr int P = first_factor(N);
+    static constexpr int M = N / P;
+    __device__ __forceinline__ static void run(float2* v) {
+        if constexpr (M == 1) {
+            base_dft<P, INV>(v);
+        } else {
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                float2 t[P];
+#pragma unroll
+                for (int p = 0; p < P; ++p) t[p] = v[m + M * p];
+                base_dft<P, INV>(t);
+#pragma unroll
+                for (int k = 0; k < P; ++k) {
+                    float2 x = t[k];
+                    if (m * k != 0) {
+                        float2 w = c_regtw[reg_tw_offset(N) + m * k];
+                        if (INV) w.y = -w.y;
+                        x = c_mul(x, w);
+                    }
+                    v[m + M * k] = x;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < P; ++k) RegFFT<M, INV>::run(v + k * M);
+        }
+    }
+};
+
+__host__ __device__ constexpr int best_split_n1(int n) {
+    // largest divisor d <= sqrt(n) with n / d <= 64; 0 when none
+    int best = 0;
+    for (int d = 2; d * d <= n; ++d)
+        if (n % d == 0 && n / d <= 64) best = d;
+    return best;
+}
+
+// Pass 1 of the four-step FFT for one (vector, n2): in-place on shared memory `x` with element
+// stride ES. `tw` is the N-point table exp(-2 pi i e / N) (global, read through L1).
+template <int N1, int N2, bool INV>
+__device__ __forceinline__ void fourstep_pass1(float2* x, int es, int n2, const float2* __restrict__ tw) {
+    constexpr int N = N1 * N2;
+    float2 v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) v[n1] = x[(n2 + N2 * n1) * es];
+    RegFFT<N1, INV>::run(v);
+    static_for<0, N1>([&](auto kc) {
+        constexpr int k1 = decltype(kc)::value;
+        constexpr int pr = reg_perm(N1, k1);
+        float2 y = v[pr];
+        if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<INV>(tw, n2 * k1));
+        x[(n2 + N2 * k1) * es] = y;
+    });
+    (void)N;
 }
 
 }  // namespace acq

@@ -172,6 +172,120 @@ __global__ void k_col_simple(const float2* __restrict__ T, int ndop, int spc, in
     }
 }
 
+// ------------------------------------------------------------------ specialised hot sizes
+// Coherent tile with the two-pass register FFT (F = N1 * N2): same mathematics as k_tile,
+// NF inverse FFTs per round; pass 1 forms S_g .* C*_m on the fly, pass 2 writes the first bs
+// lags of each row straight to the tile.
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, const float2* __restrict__ C,
+                                                 const int* __restrict__ slots, int G, int nb, int bs, int spc,
+                                                 const float2* __restrict__ twF, int NF, float inv_F,
+                                                 float2* __restrict__ T) {
+    constexpr int F = N1 * N2;
+    extern __shared__ float2 sm[];
+    float2* sg = sm;
+    float2* buf = sm + F;
+    const int g = blockIdx.x;
+    const int pi = blockIdx.y;
+    const int slot = slots[pi];
+    const int k = g % nb;
+    const float2* Sg = S + static_cast<int64_t>(g) * F;
+    for (int t = threadIdx.x; t < F; t += blockDim.x) sg[t] = Sg[t];
+    __syncthreads();
+    float2* trow = T + (static_cast<int64_t>(pi) * G + g) * spc;
+    for (int m0 = 0; m0 < nb; m0 += NF) {
+        const int nf = min(NF, nb - m0);
+        for (int task = threadIdx.x; task < nf * N2; task += blockDim.x) {
+            const int f = task / N2, n2 = task - f * N2;
+            const float2* Cm = C + (static_cast<int64_t>(slot) * nb + m0 + f) * F;
+            float2* x = buf + f * F;
+            float2 v[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; ++n1) {
+                const int n = n2 + N2 * n1;
+                v[n1] = c_mul(sg[n], __ldg(Cm + n));
+            }
+            RegFFT<N1, true>::run(v);
+            static_for<0, N1>([&](auto kc) {
+                constexpr int k1 = decltype(kc)::value;
+                constexpr int pr = reg_perm(N1, k1);
+                float2 y = v[pr];
+                if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(twF, n2 * k1));
+                x[n2 + N2 * k1] = y;
+            });
+        }
+        __syncthreads();
+        for (int task = threadIdx.x; task < nf * N1; task += blockDim.x) {
+            const int f = task / N1, k1 = task - f * N1;
+            const float2* x = buf + f * F;
+            float2 v[N2];
+#pragma unroll
+            for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[N2 * k1 + n2];
+            RegFFT<N2, true>::run(v);
+            int r = m0 + f - k;
+            if (r < 0) r += nb;
+            float2* dst = trow + r * bs;
+            static_for<0, N2>([&](auto kc) {
+                constexpr int k2 = decltype(kc)::value;
+                constexpr int pr = reg_perm(N2, k2);
+                const int j = k1 + N1 * k2;
+                if (j < bs) {
+                    const float2 y = v[pr];
+                    dst[j] = make_float2(y.x * inv_F, y.y * inv_F);
+                }
+            });
+        }
+        __syncthreads();
+    }
+}
+
+// Simple column stage with the two-pass register FFT (ndop = N1 * N2): in place in shared
+// memory, |X|^2, fftshift and the destination-row drift scatter fused into pass 2.
+template <int N1, int N2>
+__global__ void __launch_bounds__(256) k_col_simple_fs(const float2* __restrict__ T, int spc, int W,
+                                                       const float2* __restrict__ twD, const int* __restrict__ drift,
+                                                       int first, float* __restrict__ acc, int spc_eff) {
+    constexpr int ND = N1 * N2;
+    extern __shared__ float2 sm[];
+    const int pi = blockIdx.y;
+    const int c0 = blockIdx.x * W;
+    const int wv = min(W, spc - c0);
+    const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
+    for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
+        const int e = w / W, t = w - e * W;
+        sm[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int task = threadIdx.x; task < N2 * W; task += blockDim.x) {
+        const int n2 = task / W, t = task - n2 * W;
+        fourstep_pass1<N1, N2, false>(sm + t, W, n2, twD);
+    }
+    __syncthreads();
+    constexpr int half = ND / 2;
+    float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
+    for (int task = threadIdx.x; task < N1 * W; task += blockDim.x) {
+        const int k1 = task / W, t = task - k1 * W;
+        if (t >= wv) continue;
+        float2 v[N2];
+#pragma unroll
+        for (int n2 = 0; n2 < N2; ++n2) v[n2] = sm[(N2 * k1 + n2) * W + t];
+        RegFFT<N2, false>::run(v);
+        static_for<0, N2>([&](auto kc) {
+            constexpr int k2 = decltype(kc)::value;
+            constexpr int pr = reg_perm(N2, k2);
+            const int e = k1 + N1 * k2;
+            const float2 x = v[pr];
+            const float p = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+            int row = e + half;
+            if (row >= ND) row -= ND;
+            int dc = c0 + t + drift[row];
+            if (dc >= spc) dc -= spc;
+            float* cell = ap + static_cast<int64_t>(row) * spc_eff + dc;
+            *cell = first ? p : *cell + p;
+        });
+    }
+}
+
 // Destination-row update of the sign/rotation stage (top/bottom half swap of
 // src/noncoherent_integration.jl:92-113 and :267-293, including the odd-ndop quirk where raw
 // bins 0 and ndop-1 both land on row ndop/2 and row ndop-1 is never written).

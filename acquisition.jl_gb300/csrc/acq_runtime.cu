@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -82,10 +83,52 @@ FftDesc make_fft_desc(int n, DevBuf& tw) {
     return d;
 }
 
+// Register-FFT twiddles W_n^e for n = 2..kRegTwMax (constant memory, per device).
+void upload_reg_twiddles() {
+    std::vector<float2> h(kRegTwEntries);
+    for (int n = 2; n <= kRegTwMax; ++n)
+        for (int e = 0; e < n; ++e) {
+            double a = -2.0 * M_PI * static_cast<double>(e) / static_cast<double>(n);
+            h[reg_tw_offset(n) + e] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+        }
+    CK(cudaMemcpyToSymbol(c_regtw, h.data(), sizeof(float2) * h.size()));
+}
+
+using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float,
+                          float2*);
+using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, float*, int);
+
+#define ACQ_TILE_CASE(F) \
+    case F: return &k_tile_fs<best_split_n1(F), F / best_split_n1(F)>;
+#define ACQ_COL_CASE(N) \
+    case N: return &k_col_simple_fs<best_split_n1(N), N / best_split_n1(N)>;
+
+TileFsFn pick_tile_fs(int F) {
+    switch (F) {
+        ACQ_TILE_CASE(128) ACQ_TILE_CASE(256) ACQ_TILE_CASE(500) ACQ_TILE_CASE(1000) ACQ_TILE_CASE(1250)
+        ACQ_TILE_CASE(1280) ACQ_TILE_CASE(1600) ACQ_TILE_CASE(2500)
+        default: return nullptr;
+    }
+}
+
+ColFsFn pick_col_fs(int ndop) {
+    switch (ndop) {
+        ACQ_COL_CASE(16) ACQ_COL_CASE(20) ACQ_COL_CASE(32) ACQ_COL_CASE(40) ACQ_COL_CASE(64) ACQ_COL_CASE(75)
+        ACQ_COL_CASE(100) ACQ_COL_CASE(160) ACQ_COL_CASE(200) ACQ_COL_CASE(240) ACQ_COL_CASE(320) ACQ_COL_CASE(400)
+        ACQ_COL_CASE(500) ACQ_COL_CASE(640) ACQ_COL_CASE(800) ACQ_COL_CASE(1280)
+        default: return nullptr;
+    }
+}
+
 int pow2_floor(int x) {
     int p = 1;
     while (p * 2 <= x) p *= 2;
     return p;
+}
+
+bool getenv_flag(const char* name) {
+    const char* v = std::getenv(name);
+    return v && v[0] && v[0] != '0';
 }
 
 size_t sample_bytes(int dtype) {
@@ -117,6 +160,11 @@ struct acq_plan {
     DevBuf input, S, T, accb, winb, rowpart, colsum, peakpart, zs, res, slots, prn_ids;
     int tileB = 1, Wsimple = 1, Wsign = 1, nct = 1;
     size_t smem_front = 0, smem_tile = 0, smem_simple = 0, smem_sign = 0;
+    // specialised two-pass FFT kernels for the plan's sizes (nullptr: generic kernels)
+    TileFsFn tile_fs = nullptr;
+    ColFsFn col_fs = nullptr;
+    int tileNF = 1, Wfs = 1;
+    size_t smem_tile_fs = 0, smem_col_fs = 0;
     // last acquisition
     int last_n = 0;
     uint32_t last_flags = 0;
@@ -197,6 +245,21 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     set_smem((const void*)k_col_simple, P->smem_simple);
     set_smem((const void*)k_col_sign, P->smem_sign);
     set_smem((const void*)k_col_rot, P->smem_sign);
+    upload_reg_twiddles();
+    if (!getenv_flag("ACQ_GENERIC_FFT")) {
+        P->tile_fs = pick_tile_fs(g.fft_size);
+        P->col_fs = g.path == 0 ? pick_col_fs(g.ndop) : nullptr;
+    }
+    if (P->tile_fs) {
+        P->tileNF = std::max(1, std::min(g.nb, static_cast<int>(48 * 1024 / (sizeof(float2) * g.fft_size)) - 1));
+        P->smem_tile_fs = sizeof(float2) * g.fft_size * (1 + P->tileNF);
+        set_smem((const void*)P->tile_fs, P->smem_tile_fs);
+    }
+    if (P->col_fs) {
+        P->Wfs = g.ndop <= 400 ? 32 : g.ndop <= 800 ? 16 : 8;
+        P->smem_col_fs = sizeof(float2) * g.ndop * P->Wfs;
+        set_smem((const void*)P->col_fs, P->smem_col_fs);
+    }
     P->nct = (g.spc_eff + kStatsCols - 1) / kStatsCols;
 
     // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
@@ -315,14 +378,23 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
     for (int m = 0; m < g.n_nc; ++m) {
         const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_size;
         t_begin(P, ACQ_KERNEL_TILE);
-        k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb, g.bs,
-                                                           g.spc, P->fftF, P->tileB, inv_F, P->T.as<float2>());
+        if (P->tile_fs)
+            P->tile_fs<<<dim3(G, n), kThreads, P->smem_tile_fs, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G,
+                                                                     g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF, inv_F,
+                                                                     P->T.as<float2>());
+        else
+            k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb,
+                                                               g.bs, g.spc, P->fftF, P->tileB, inv_F, P->T.as<float2>());
         t_end(P);
         ++L;
         const int* dr = P->drift.as<int>() + (size_t)m * g.ndop;
         const int first = m == 0;
         t_begin(P, ACQ_KERNEL_COLUMN);
-        if (g.path == 0) {
+        if (g.path == 0 && P->col_fs) {
+            const int W = P->Wfs;
+            P->col_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_col_fs, st>>>(
+                P->T.as<float2>(), g.spc, W, P->fftD.tw, dr, first, P->accb.as<float>(), g.spc_eff);
+        } else if (g.path == 0) {
             const int W = P->Wsimple;
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
