@@ -62,9 +62,11 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_plan_doppler_freqs", "acq_acquire", "acq_acquire_device_async", "acq_fetch_results",
             "acq_plan_stream", "acq_plan_last_launch_count", "acq_cfar_threshold", "acq_gen_code",
             "acq_last_error", "acq_version", "acq_plan_set_kernel_timing", "acq_plan_kernel_times",
-            "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc"]
+            "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc", "acq_plan_set_option"]
+ACQ_OPT_FORM = 0
+ACQ_FORM_FUSED, ACQ_FORM_PLAIN = 0, 1
 KERNEL_KINDS = 8
-KERNEL_NAMES = ["frontend", "tile", "column", "stats", "extract", "secondary", "k6", "k7"]
+KERNEL_NAMES = ["frontend", "tile", "column", "stats", "extract", "secondary", "fused", "k7"]
 
 _lib = None
 
@@ -103,6 +105,7 @@ def load():
     lib.acq_plan_reset_kernel_times.argtypes = [P]
     lib.acq_est_signal_noise_power_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_double,
                                                        C.c_int32, C.c_void_p, C.c_void_p]
+    lib.acq_plan_set_option.argtypes = [P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
     lib.acq_version.restype = C.c_char_p
     for name in EXPORTED:
         if name not in ("acq_plan_desc_init", "acq_version"):

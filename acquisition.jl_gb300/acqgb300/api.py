@@ -229,6 +229,14 @@ class AcquisitionPlan:
         _check(L.load().acq_plan_last_launch_count(self._h, C.byref(n)))
         return n.value
 
+    def set_form(self, form: str) -> str:
+        """'plain' (one kernel per stage, the default) or 'fused' (cluster kernel where supported).
+        Returns the form in effect."""
+        val = {"fused": L.ACQ_FORM_FUSED, "plain": L.ACQ_FORM_PLAIN}[form]
+        eff = C.c_int64()
+        _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_FORM, val, C.byref(eff)))
+        return "fused" if eff.value == L.ACQ_FORM_FUSED else "plain"
+
     def set_kernel_timing(self, enable: bool = True):
         _check(L.load().acq_plan_set_kernel_timing(self._h, 1 if enable else 0))
 

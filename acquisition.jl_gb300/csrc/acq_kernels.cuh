@@ -2,6 +2,7 @@
 // it replaces (paths inside JuliaGNSS/Acquisition.jl v2.6.4).
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cstdint>
 
 #include "acq_fft.cuh"
@@ -244,9 +245,10 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
 template <int N1, int N2>
 __global__ void __launch_bounds__(256) k_col_simple_fs(const float2* __restrict__ T, int spc, int W,
                                                        const float2* __restrict__ twD, const int* __restrict__ drift,
-                                                       int first, float* __restrict__ acc, int spc_eff) {
+                                                       int first, int has_drift, float* __restrict__ acc, int spc_eff) {
     constexpr int ND = N1 * N2;
     extern __shared__ float2 sm[];
+    int* dr = reinterpret_cast<int*>(sm + ND * W);
     const int pi = blockIdx.y;
     const int c0 = blockIdx.x * W;
     const int wv = min(W, spc - c0);
@@ -255,6 +257,7 @@ __global__ void __launch_bounds__(256) k_col_simple_fs(const float2* __restrict_
         const int e = w / W, t = w - e * W;
         sm[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
     }
+    for (int i = threadIdx.x; i < ND; i += blockDim.x) dr[i] = has_drift ? drift[i] : 0;
     __syncthreads();
     for (int task = threadIdx.x; task < N2 * W; task += blockDim.x) {
         const int n2 = task / W, t = task - n2 * W;
@@ -266,23 +269,180 @@ __global__ void __launch_bounds__(256) k_col_simple_fs(const float2* __restrict_
     for (int task = threadIdx.x; task < N1 * W; task += blockDim.x) {
         const int k1 = task / W, t = task - k1 * W;
         if (t >= wv) continue;
+        const int c = c0 + t;
         float2 v[N2];
 #pragma unroll
         for (int n2 = 0; n2 < N2; ++n2) v[n2] = sm[(N2 * k1 + n2) * W + t];
         RegFFT<N2, false>::run(v);
+        // power in natural order, then the accumulator cells: loads batched ahead of the stores
+        float p[N2];
+        int64_t idx[N2];
         static_for<0, N2>([&](auto kc) {
             constexpr int k2 = decltype(kc)::value;
             constexpr int pr = reg_perm(N2, k2);
-            const int e = k1 + N1 * k2;
             const float2 x = v[pr];
-            const float p = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
-            int row = e + half;
+            p[k2] = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+            int row = k1 + N1 * k2 + half;
             if (row >= ND) row -= ND;
-            int dc = c0 + t + drift[row];
+            int dc = c + dr[row];
             if (dc >= spc) dc -= spc;
-            float* cell = ap + static_cast<int64_t>(row) * spc_eff + dc;
-            *cell = first ? p : *cell + p;
+            idx[k2] = static_cast<int64_t>(row) * spc_eff + dc;
         });
+        if (first) {
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) ap[idx[k2]] = p[k2];
+        } else {
+            float old[N2];
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) old[k2] = ap[idx[k2]];
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) ap[idx[k2]] = __fadd_rn(old[k2], p[k2]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ fused simple path
+// One thread-block cluster of CL CTAs per (requested PRN, column block r) runs every
+// accumulation step of the simple path without touching HBM in between:
+//   1. CTA q inverse-FFTs its rows g in [q*RPC, (q+1)*RPC) (F = N1F*N2F, S_g .* C*_{(k+r) mod nb})
+//      and stores lag j of row g into the shared memory of the CTA that owns column j
+//      (distributed shared memory, columns [q*CPC, (q+1)*CPC) belong to CTA q);
+//   2. after a cluster barrier each CTA runs the Doppler FFT (ndop = N1D*N2D) down its CPC
+//      columns and adds |X|^2 (fftshift, destination-row drift) into a shared-memory
+//      accumulator with an H-column halo on each side;
+//   3. after the last step interior columns are stored, halo/edge columns are atomically added
+//      to the (zeroed) global accumulator.
+// Same mathematics as k_tile + k_col_simple_fs; the per-cell step order of the sums is kept.
+struct FusedParams {
+    int G, nb, bs, spc, spc_eff, n_nc, rpc, cpc, nf, halo;
+    float inv_F;
+    const float2* S;       // (n_nc, G, F)
+    const float2* C;       // (slots, nb, F)
+    const int* slots;
+    const float2* twF;
+    const float2* twD;
+    const int* drift;      // (n_nc, ndop) in [0, spc)
+    float* acc;            // (n_req, ndop, spc_eff)
+};
+
+template <int N1F, int N2F, int N1D, int N2D>
+__global__ void __launch_bounds__(256) k_fused_simple(FusedParams fp) {
+    namespace cg = cooperative_groups;
+    constexpr int F = N1F * N2F;
+    constexpr int ND = N1D * N2D;
+    constexpr int NW = 8;                       // warps per CTA (256 threads)
+    cg::cluster_group cluster = cg::this_cluster();
+    const int q = static_cast<int>(cluster.block_rank());
+    const int CL = static_cast<int>(cluster.num_blocks());
+    const int r = blockIdx.x / CL;
+    const int pi = blockIdx.y;
+    const int slot = fp.slots[pi];
+    const int CPC = fp.cpc, H = fp.halo, AW = fp.cpc + 2 * fp.halo;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    extern __shared__ float2 sm[];
+    float2* tile = sm;                                         // ND x CPC, written by every CTA of the cluster
+    float2* wbuf = tile + ND * CPC + wid * F;                  // this warp's FFT buffer (NW x F)
+    float* accl = reinterpret_cast<float*>(tile + ND * CPC + NW * F);   // ND x AW
+    int* dr = reinterpret_cast<int*>(accl + ND * AW);          // this step's signed drift per sorted row
+    const int g0 = q * fp.rpc, g1 = min(ND, g0 + fp.rpc);
+    const int j0 = q * CPC;
+    const int wv = max(0, min(CPC, fp.bs - j0));
+    const int cpw = (CPC + NW - 1) / NW;                       // Doppler columns per warp
+    for (int i = threadIdx.x; i < ND * AW; i += blockDim.x) accl[i] = 0.f;
+    cluster.sync();   // every CTA of the cluster is running before any remote store
+    constexpr int half = ND / 2;
+    for (int m = 0; m < fp.n_nc; ++m) {
+        const float2* Sm = fp.S + static_cast<int64_t>(m) * fp.G * F;
+        for (int i = threadIdx.x; i < ND; i += blockDim.x) {
+            int sh = fp.drift[m * ND + i];
+            if (sh > fp.spc / 2) sh -= fp.spc;       // signed drift, |sh| <= H
+            dr[i] = sh;
+        }
+        // ---- inverse FFTs: warp wid owns rows g0+wid, g0+wid+NW, ...; lags go to their owner CTA
+        for (int g = g0 + wid; g < g1; g += NW) {
+            const int cm = (g % fp.nb + r) % fp.nb;
+            const float2* Sg = Sm + static_cast<int64_t>(g) * F;
+            const float2* Cm = fp.C + (static_cast<int64_t>(slot) * fp.nb + cm) * F;
+            for (int n2 = lane; n2 < N2F; n2 += 32) {
+                float2 v[N1F];
+#pragma unroll
+                for (int n1 = 0; n1 < N1F; ++n1) {
+                    const int n = n2 + N2F * n1;
+                    v[n1] = c_mul(__ldg(Sg + n), __ldg(Cm + n));
+                }
+                RegFFT<N1F, true>::run(v);
+                static_for<0, N1F>([&](auto kc) {
+                    constexpr int k1 = decltype(kc)::value;
+                    constexpr int pr = reg_perm(N1F, k1);
+                    float2 y = v[pr];
+                    if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(fp.twF, n2 * k1));
+                    wbuf[n2 + N2F * k1] = y;
+                });
+            }
+            __syncwarp();
+            for (int k1 = lane; k1 < N1F; k1 += 32) {
+                float2 v[N2F];
+#pragma unroll
+                for (int n2 = 0; n2 < N2F; ++n2) v[n2] = wbuf[N2F * k1 + n2];
+                RegFFT<N2F, true>::run(v);
+                static_for<0, N2F>([&](auto kc) {
+                    constexpr int k2 = decltype(kc)::value;
+                    constexpr int pr = reg_perm(N2F, k2);
+                    const int j = k1 + N1F * k2;
+                    if (j < fp.bs) {
+                        const int owner = j / CPC;
+                        float2* dst = cluster.map_shared_rank(tile, owner);
+                        const float2 y = v[pr];
+                        dst[g * CPC + (j - owner * CPC)] = make_float2(y.x * fp.inv_F, y.y * fp.inv_F);
+                    }
+                });
+            }
+            __syncwarp();
+        }
+        cluster.sync();
+        // ---- Doppler FFT: warp wid owns columns [wid*cpw, (wid+1)*cpw); each destination cell gets
+        // exactly one contribution per step (the drift scatter is a bijection per row)
+        const int t0 = wid * cpw, t1 = min(wv, t0 + cpw);
+        const int ncw = max(0, t1 - t0);
+        for (int task = lane; task < N2D * ncw; task += 32) {
+            const int n2 = task / ncw, t = t0 + (task - n2 * ncw);
+            fourstep_pass1<N1D, N2D, false>(tile + t, CPC, n2, fp.twD);
+        }
+        __syncwarp();
+        for (int task = lane; task < N1D * ncw; task += 32) {
+            const int k1 = task / ncw, t = t0 + (task - k1 * ncw);
+            float2 v[N2D];
+#pragma unroll
+            for (int n2 = 0; n2 < N2D; ++n2) v[n2] = tile[(N2D * k1 + n2) * CPC + t];
+            RegFFT<N2D, false>::run(v);
+            static_for<0, N2D>([&](auto kc) {
+                constexpr int k2 = decltype(kc)::value;
+                constexpr int pr = reg_perm(N2D, k2);
+                const float2 xv = v[pr];
+                const float p = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
+                int row = k1 + N1D * k2 + half;
+                if (row >= ND) row -= ND;
+                float* cell = accl + row * AW + H + t + dr[row];
+                *cell = __fadd_rn(*cell, p);
+            });
+        }
+        cluster.sync();   // every CTA is done with its tile (and dr) before the next step overwrites it
+    }
+    // ---- write back: interior columns are owned, halo/edge columns are shared with neighbours
+    float* ap = fp.acc + static_cast<int64_t>(pi) * ND * fp.spc_eff;
+    const int cbase = r * fp.bs + j0;
+    const int lo = -H, hi = wv + H;
+    const int span = hi - lo;
+    for (int i = threadIdx.x; i < ND * span; i += blockDim.x) {
+        const int row = i / span;
+        const int lc = lo + (i - row * span);
+        const float v = accl[row * AW + H + lc];
+        int c = cbase + lc;
+        if (c < 0) c += fp.spc;
+        if (c >= fp.spc) c -= fp.spc;
+        float* cell = ap + static_cast<int64_t>(row) * fp.spc_eff + c;
+        if (H == 0 || (lc >= H && lc < wv - H)) *cell = v;
+        else if (v != 0.f) atomicAdd(cell, v);
     }
 }
 

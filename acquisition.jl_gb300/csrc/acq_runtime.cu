@@ -96,7 +96,7 @@ void upload_reg_twiddles() {
 
 using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float,
                           float2*);
-using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, float*, int);
+using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, int, float*, int);
 
 #define ACQ_TILE_CASE(F) \
     case F: return &k_tile_fs<best_split_n1(F), F / best_split_n1(F)>;
@@ -118,6 +118,19 @@ ColFsFn pick_col_fs(int ndop) {
         ACQ_COL_CASE(500) ACQ_COL_CASE(640) ACQ_COL_CASE(800) ACQ_COL_CASE(1280)
         default: return nullptr;
     }
+}
+
+using FusedFn = void (*)(FusedParams);
+
+#define ACQ_FUSED_CASE(F, D)                                                                  \
+    if (fft == F && ndop == D)                                                                \
+        return &k_fused_simple<best_split_n1(F), F / best_split_n1(F), best_split_n1(D), D / best_split_n1(D)>;
+
+FusedFn pick_fused(int fft, int ndop) {
+    ACQ_FUSED_CASE(500, 200) ACQ_FUSED_CASE(500, 16) ACQ_FUSED_CASE(500, 20) ACQ_FUSED_CASE(256, 16)
+    ACQ_FUSED_CASE(256, 32) ACQ_FUSED_CASE(128, 32) ACQ_FUSED_CASE(1280, 75) ACQ_FUSED_CASE(2500, 20)
+    ACQ_FUSED_CASE(1250, 320) ACQ_FUSED_CASE(1250, 16) ACQ_FUSED_CASE(500, 40) ACQ_FUSED_CASE(500, 400)
+    return nullptr;
 }
 
 int pow2_floor(int x) {
@@ -164,7 +177,13 @@ struct acq_plan {
     TileFsFn tile_fs = nullptr;
     ColFsFn col_fs = nullptr;
     int tileNF = 1, Wfs = 1;
+    std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
+    // fused cluster form
+    FusedFn fused = nullptr;
+    int form = ACQ_FORM_PLAIN;
+    int fusedCL = 8, fusedRPC = 1, fusedCPC = 1, fusedNF = 1, fusedH = 0;
+    size_t smem_fused = 0;
     // last acquisition
     int last_n = 0;
     uint32_t last_flags = 0;
@@ -220,6 +239,55 @@ void t_collect(acq_plan* P) {
     P->ev_used = 0;
 }
 
+// Choose the fused cluster form when the plan's sizes have a fused kernel, its shared memory
+// fits and a cluster of that shape can be resident.
+void setup_fused(acq_plan* P) {
+    const Geometry& g = P->g;
+    P->fused = nullptr;
+    if (g.path != 0 || getenv_flag("ACQ_GENERIC_FFT")) return;
+    FusedFn fn = pick_fused(g.fft_size, g.ndop);
+    if (!fn) return;
+    // signed drift bound over all steps (src/noncoherent_integration.jl:600-619)
+    int H = 0;
+    std::vector<int32_t> dr(g.ndop);
+    for (int m = 0; m < g.n_nc; ++m) {
+        code_drift_shifts(g, *P->sys, P->desc.sampling_freq_hz, m, dr.data());
+        for (int v : dr) H = std::max(H, std::min(v, g.spc - v));
+    }
+    const int CL = 8;
+    const int rpc = (g.ndop + CL - 1) / CL;
+    const int cpc = (g.bs + CL - 1) / CL;
+    if (H > cpc) return;
+    const int nf = 8;   // one FFT buffer per warp
+    const size_t smem = sizeof(float2) * (size_t)g.ndop * cpc + sizeof(float2) * (size_t)nf * g.fft_size +
+                        sizeof(float) * (size_t)g.ndop * (cpc + 2 * H) + sizeof(int) * (size_t)g.ndop;
+    if (smem > 220 * 1024) return;
+    set_smem((const void*)fn, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.nb * CL, 1, 1);
+    cfg.blockDim = dim3(kThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)fn, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();
+        return;
+    }
+    P->fused = fn;
+    P->fusedCL = CL;
+    P->fusedRPC = rpc;
+    P->fusedCPC = cpc;
+    P->fusedNF = nf;
+    P->fusedH = H;
+    P->smem_fused = smem;
+}
+
 void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
     const Geometry& g = P->g;
     CK(cudaSetDevice(P->device));
@@ -252,15 +320,18 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     }
     if (P->tile_fs) {
         P->tileNF = std::max(1, std::min(g.nb, static_cast<int>(48 * 1024 / (sizeof(float2) * g.fft_size)) - 1));
+        if (const char* e = std::getenv("ACQ_TILE_NF")) P->tileNF = std::max(1, std::min(g.nb, std::atoi(e)));
         P->smem_tile_fs = sizeof(float2) * g.fft_size * (1 + P->tileNF);
         set_smem((const void*)P->tile_fs, P->smem_tile_fs);
     }
     if (P->col_fs) {
         P->Wfs = g.ndop <= 400 ? 32 : g.ndop <= 800 ? 16 : 8;
-        P->smem_col_fs = sizeof(float2) * g.ndop * P->Wfs;
+        if (const char* e = std::getenv("ACQ_COL_W")) P->Wfs = std::max(1, std::min(64, std::atoi(e)));
+        P->smem_col_fs = sizeof(float2) * g.ndop * P->Wfs + sizeof(int) * g.ndop;
         set_smem((const void*)P->col_fs, P->smem_col_fs);
     }
     P->nct = (g.spc_eff + kStatsCols - 1) / kStatsCols;
+    setup_fused(P);
 
     // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
     std::vector<int8_t> h_codes(static_cast<size_t>(n_prns) * g.spc);
@@ -307,6 +378,10 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     // drift shifts per step, src/noncoherent_integration.jl:600-619
     std::vector<int32_t> dr((size_t)g.n_nc * g.ndop);
     for (int m = 0; m < g.n_nc; ++m) code_drift_shifts(g, *P->sys, P->desc.sampling_freq_hz, m, &dr[(size_t)m * g.ndop]);
+    P->step_has_drift.assign(g.n_nc, 0);
+    for (int m = 0; m < g.n_nc; ++m)
+        for (int r = 0; r < g.ndop; ++r)
+            if (dr[(size_t)m * g.ndop + r] != 0) P->step_has_drift[m] = 1;
     P->drift.ensure(sizeof(int32_t) * dr.size());
     CK(cudaMemcpy(P->drift.p, dr.data(), sizeof(int32_t) * dr.size(), cudaMemcpyHostToDevice));
     // per-acquisition buffers sized for all plan PRNs
@@ -375,7 +450,33 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
     t_end(P);
     ++L;
     const float inv_F = 1.0f / static_cast<float>(g.fft_size);
-    for (int m = 0; m < g.n_nc; ++m) {
+    const bool use_fused = P->fused && P->form == ACQ_FORM_FUSED;
+    if (use_fused) {
+        if (P->fusedH > 0)
+            CK(cudaMemsetAsync(P->accb.p, 0, sizeof(float) * (size_t)n * g.ndop * g.spc_eff, st));
+        FusedParams fp{};
+        fp.G = G; fp.nb = g.nb; fp.bs = g.bs; fp.spc = g.spc; fp.spc_eff = g.spc_eff; fp.n_nc = g.n_nc;
+        fp.rpc = P->fusedRPC; fp.cpc = P->fusedCPC; fp.nf = P->fusedNF; fp.halo = P->fusedH; fp.inv_F = inv_F;
+        fp.S = P->S.as<float2>(); fp.C = P->conj.as<float2>(); fp.slots = P->slots.as<int>();
+        fp.twF = P->fftF.tw; fp.twD = P->fftD.tw; fp.drift = P->drift.as<int>(); fp.acc = P->accb.as<float>();
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(g.nb * P->fusedCL, n, 1);
+        cfg.blockDim = dim3(kThreads, 1, 1);
+        cfg.dynamicSmemBytes = P->smem_fused;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = P->fusedCL;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        t_begin(P, ACQ_KERNEL_FUSED);
+        CK(cudaLaunchKernelEx(&cfg, P->fused, fp));
+        t_end(P);
+        ++L;
+    }
+    for (int m = 0; m < (use_fused ? 0 : g.n_nc); ++m) {
         const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_size;
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
@@ -393,7 +494,8 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
         if (g.path == 0 && P->col_fs) {
             const int W = P->Wfs;
             P->col_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_col_fs, st>>>(
-                P->T.as<float2>(), g.spc, W, P->fftD.tw, dr, first, P->accb.as<float>(), g.spc_eff);
+                P->T.as<float2>(), g.spc, W, P->fftD.tw, dr, first, P->step_has_drift[m], P->accb.as<float>(),
+                g.spc_eff);
         } else if (g.path == 0) {
             const int W = P->Wsimple;
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
@@ -664,6 +766,17 @@ int acq_plan_reset_kernel_times(acq_plan* P) {
             P->kt_ms[i] = 0;
             P->kt_n[i] = 0;
         }
+    });
+}
+
+int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* effective) {
+    return guarded([&] {
+        if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (option != ACQ_OPT_FORM) throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
+        if (value != ACQ_FORM_FUSED && value != ACQ_FORM_PLAIN)
+            throw AcqError(ACQ_ERR_ARGUMENT, "unknown form " + std::to_string(value));
+        P->form = static_cast<int>(value);
+        if (effective) *effective = (P->fused && P->form == ACQ_FORM_FUSED) ? ACQ_FORM_FUSED : ACQ_FORM_PLAIN;
     });
 }
 

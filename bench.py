@@ -157,6 +157,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="plain", choices=["fused", "plain"],
+                    help="kernel form of the headline measurement (the other form is reported beside it)")
     ap.add_argument("--accumulations", type=int, default=N_NC,
                     help="non-coherent accumulations (profiling cases only; the workload uses 8)")
     args = ap.parse_args()
@@ -184,6 +186,8 @@ def main():
     n_nc = args.accumulations
     plan = A.plan_acquire(A.GPSL1CA(), FS, PRNS, min_doppler_coverage=COV, num_coherently_integrated_code_periods=N_COH,
                           num_noncoherent_accumulations=n_nc, device=local_rank)
+    main_form = plan.set_form(args.form)
+    other_form = "plain" if main_form == "fused" else "fused"
     host = torch.from_numpy(ci16).pin_memory()
     dev = host.to(f"cuda:{local_rank}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
@@ -228,6 +232,36 @@ def main():
         t_step = float(t.item())
     value = world * 1.0 / t_step
 
+    # ---- the other form on the same input (plain: one kernel per stage, tile and accumulator
+    # in HBM; fused: the cluster kernel)
+    form = main_form
+    plain_value = None
+    if plan.set_form(other_form) == other_form:
+        for _ in range(2):
+            A.acquire_device(plan, dev, PRNS)
+        pm = []
+        for _ in range(args.steps):
+            flush_l2()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(pstream)
+            A.acquire_device_async(plan, dev, PRNS)
+            e1.record(pstream)
+            A.fetch_results(plan, PRNS)
+            pm.append(e0.elapsed_time(e1))
+        plain_value = world * 1e3 / statistics.mean(pm)
+        plan.set_kernel_timing(True)
+        plan.reset_kernel_times()
+        for _ in range(args.steps):
+            flush_l2()
+            A.acquire_device_async(plan, dev, PRNS)
+            A.fetch_results(plan, PRNS)
+        plain_ktimes = plan.kernel_times()
+        plan.set_kernel_timing(False)
+        plan.set_form(main_form)
+    else:
+        plain_ktimes = None
+
     # ---- per-kernel device time (same workload, events around every launch)
     plan.set_kernel_timing(True)
     plan.reset_kernel_times()
@@ -271,6 +305,15 @@ def main():
         "column": n_prn * ndop * spc * 8 + n_prn * ndop * spc * 4 * 2,              # T read + acc read/write
         "frontend": n_nc * N_COH * spc * 4 + n_nc * ndop * F * 8,
         "stats": n_prn * ndop * spc * 4,
+        # fused: input spectra + code spectra reads, one accumulator write (the algorithmic minimum)
+        "fused": n_nc * ndop * F * 8 + n_prn * nb * F * 8 + n_prn * ndop * spc * 4,
+    }
+    # FP32 FFT work per launch (5 N log2 N per complex FFT + 6 per complex multiply)
+    fft_flops = lambda n: 5.0 * n * math.log2(n)
+    flops = {
+        "tile": n_prn * ndop * nb * (fft_flops(F) + 6 * F),
+        "column": n_prn * spc * (fft_flops(ndop) + 3 * ndop),
+        "fused": n_nc * n_prn * (ndop * nb * (fft_flops(F) + 6 * F) + spc * (fft_flops(ndop) + 3 * ndop)),
     }
     ab = alg_bytes.get(name)
     achieved = ab / per_launch_s / 1e9 if ab else None
@@ -278,6 +321,7 @@ def main():
             "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
             "per_launch_ms": per_launch_s * 1e3, "algorithmic_bytes_per_launch": ab,
+            "fp32_tflops": (flops[name] / per_launch_s / 1e12) if name in flops else None,
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()}}
 
     cpu = None
@@ -293,9 +337,12 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, CI16)",
             "config": {"workload": WORKLOAD if n_nc == N_NC else f"{WORKLOAD}_nnc{n_nc}", "prns": n_prn, "samples": samples, "num_doppler_bins": ndop,
-                       "samples_per_code": spc, "fft_size": F, "form": "plain",
+                       "samples_per_code": spc, "fft_size": F, "form": form,
                        "l2": "flushed (256 MB write) before every timed step"},
             "msample_prn_per_s": value * n_prn * samples / 1e6,
+            "other_form": {"form": other_form, "value": plain_value, "unit": "acq/s",
+                           "kernel_ms_per_step": ({k: v[0] / args.steps for k, v in plain_ktimes.items()}
+                                                  if plain_ktimes else None)},
             "e2e": {"value": e2e_value, "unit": "acq/s", "h2d_bytes_per_step": int(ci16.nbytes),
                     "d2h_bytes_per_step": n_prn * 72, "ms_per_step": t_e2e * 1e3},
             "gpu_launches": int(launches_per_step * args.steps),

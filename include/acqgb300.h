@@ -155,6 +155,16 @@ int acq_plan_stream(const acq_plan* plan, void** stream);
 /* Number of this library's kernel launches enqueued by the last acquisition. */
 int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 
+/* Plan options (acq_plan_set_option). */
+#define ACQ_OPT_FORM 0               /* ACQ_FORM_PLAIN (default) or ACQ_FORM_FUSED */
+#define ACQ_FORM_FUSED 0             /* cluster kernel: tile + Doppler stage + accumulation in shared memory */
+#define ACQ_FORM_PLAIN 1             /* one kernel per stage, coherent tile and accumulator in HBM */
+
+/* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
+ * form is used only where the plan's sizes have a fused kernel (otherwise plain). Returns the
+ * form now in effect through `effective` (may be NULL). No reference counterpart. */
+int acq_plan_set_option(acq_plan* plan, int32_t option, int64_t value, int64_t* effective);
+
 /* Kernel classes for per-launch device timing. */
 #define ACQ_KERNEL_FRONTEND 0        /* downconversion + double-block FFT */
 #define ACQ_KERNEL_TILE 1            /* code-spectrum multiply + inverse FFT (coherent tile) */
@@ -162,6 +172,7 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_KERNEL_STATS 3           /* peak + FP64 noise partial sums */
 #define ACQ_KERNEL_EXTRACT 4         /* result extraction, CFAR gate, interpolation */
 #define ACQ_KERNEL_SECONDARY 5       /* secondary-code despread */
+#define ACQ_KERNEL_FUSED 6           /* fused tile + Doppler + accumulation (cluster kernel) */
 #define ACQ_KERNEL_KINDS 8
 
 /* Enable (1) or disable (0) CUDA-event timing of every launch of this plan (on the plan's

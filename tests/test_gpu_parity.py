@@ -28,7 +28,7 @@ SYS = {"GPSL1CA": (A.GPSL1CA, G.GPSL1CA), "GPSL5I": (A.GPSL5I, G.GPSL5I), "Galil
 
 
 def _run_case(name, fs, prns, n_coh=1, n_be=1, n_nc=1, cov=7000.0, sats=(), seed=1, interm_freq=0.0,
-              quant=None, interp=False, noise_estimator="opposite_row", use_secondary_code=True):
+              quant=None, interp=False, noise_estimator="opposite_row", use_secondary_code=True, form=None):
     a_sys, o_sys = SYS[name]
     a_sys = a_sys()
     plan = A.plan_acquire(a_sys, fs, prns, min_doppler_coverage=cov, num_coherently_integrated_code_periods=n_coh,
@@ -36,6 +36,8 @@ def _run_case(name, fs, prns, n_coh=1, n_be=1, n_nc=1, cov=7000.0, sats=(), seed
                           noise_estimator=(A.GlobalMeanNoiseEstimator() if noise_estimator == "global_mean"
                                            else A.OppositeRowNoiseEstimator()),
                           use_secondary_code=use_secondary_code)
+    if form is not None:
+        assert plan.set_form(form) == form
     n = n_nc * n_coh * plan.samples_per_code
     x = synth.synth(a_sys, fs, n, list(sats), seed, interm_freq=interm_freq)
     if quant == "ci16":
@@ -95,13 +97,33 @@ def test_cfg1_l1ca_4mhz_32prns():
     assert A.is_detected(res[0]) and abs(res[0].code_phase - 300.5) < 1.0
 
 
-def test_l1ca_multistep_drift_ci16():
+@pytest.mark.parametrize("form", ["fused", "plain"])
+def test_l1ca_multistep_drift_ci16(form):
+    # the weak-signal workload's geometry (10 ms x 8, drift reaches one sample) in both forms
     rng = np.random.default_rng(5)
-    sats = synth.random_sats(rng, [3, 9], (42, 45), 5000, 1023, 0.02)
-    plan, res, outs = _run_case("GPSL1CA", 5e6, [3, 9, 17], n_coh=10, n_nc=4, cov=5000, sats=sats, seed=5,
-                                quant="ci16")
+    sats = synth.random_sats(rng, [3, 9], (40, 44), 5000, 1023, 0.02)
+    sats[0].doppler = 4950.0
+    plan, res, outs = _run_case("GPSL1CA", 5e6, [3, 9, 17], n_coh=10, n_nc=8, cov=5000, sats=sats, seed=5,
+                                quant="ci16", form=form)
     assert plan.num_doppler_bins == 200
-    _compare(res, outs, "l1-10msx4-ci16")
+    _compare(res, outs, f"l1-10msx8-ci16-{form}")
+
+
+def test_fused_and_plain_forms_agree():
+    sats = [synth.Satellite(7, 41.0, -3300.0, 612.4)]
+    a_sys = A.GPSL1CA()
+    plan = A.plan_acquire(a_sys, 5e6, [7, 8], min_doppler_coverage=5000, num_coherently_integrated_code_periods=10,
+                          num_noncoherent_accumulations=8)
+    x = synth.to_ci16(synth.synth(a_sys, 5e6, 8 * 10 * 5000, sats, 77))
+    assert plan.set_form("fused") == "fused"
+    rf = A.acquire_b(plan, x, [7, 8], store_power_bins=True)
+    pf = [r.power_bins.copy() for r in rf]
+    assert plan.set_form("plain") == "plain"
+    rp = A.acquire_b(plan, x, [7, 8], store_power_bins=True)
+    for a, b, p in zip(rf, rp, pf):
+        assert (a.peak_doppler_bin, a.peak_code_bin) == (b.peak_doppler_bin, b.peak_code_bin)
+        assert np.abs(p - b.power_bins).max() <= 1e-5 * b.power_bins.max()
+        assert float(a.noise_power) == pytest.approx(float(b.noise_power), rel=1e-5)
 
 
 def test_l1ca_interm_freq_interp_global_mean():
