@@ -1,6 +1,8 @@
 // acq_runtime.cu — plan lifetime, device memory, launch sequence and the C ABI of
 // libacqgb300. Host logic mirrors plan_acquire / acquire! (src/plan.jl:312-697,
 // src/acquire.jl:54-215); all per-sample work runs in the kernels of acq_kernels.cuh.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -95,7 +97,35 @@ void upload_reg_twiddles() {
 }
 
 using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float,
-                          float2*);
+                          float2*, int64_t, int);
+using ColTmaFn = void (*)(const CUtensorMap, ColTmaParams);
+
+#define ACQ_COLTMA_CASE(N) \
+    case N: return &k_col_tma<best_split_n1(N), N / best_split_n1(N)>;
+
+ColTmaFn pick_col_tma(int ndop) {
+    switch (ndop) {
+        ACQ_COLTMA_CASE(16) ACQ_COLTMA_CASE(20) ACQ_COLTMA_CASE(32) ACQ_COLTMA_CASE(40) ACQ_COLTMA_CASE(64)
+        ACQ_COLTMA_CASE(75) ACQ_COLTMA_CASE(100) ACQ_COLTMA_CASE(160) ACQ_COLTMA_CASE(200) ACQ_COLTMA_CASE(240)
+        ACQ_COLTMA_CASE(320) ACQ_COLTMA_CASE(400) ACQ_COLTMA_CASE(500)
+        default: return nullptr;
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
 using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, int, float*, int);
 
 #define ACQ_TILE_CASE(F) \
@@ -176,9 +206,15 @@ struct acq_plan {
     // specialised two-pass FFT kernels for the plan's sizes (nullptr: generic kernels)
     TileFsFn tile_fs = nullptr;
     ColFsFn col_fs = nullptr;
-    int tileNF = 1, Wfs = 1;
+    int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1;
     std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
+    // TMA-staged column stage over all steps (simple path)
+    ColTmaFn col_tma = nullptr;
+    CUtensorMap tmapT{};
+    DevBuf Tall, errflag;
+    int tmaW = 16, tmaBoxRows = 1, tmaBoxes = 1, tmaGrid = 1, tmaH = 0;
+    size_t smem_col_tma = 0;
     // fused cluster form
     FusedFn fused = nullptr;
     int form = ACQ_FORM_PLAIN;
@@ -288,6 +324,64 @@ void setup_fused(acq_plan* P) {
     P->smem_fused = smem;
 }
 
+// TMA-staged column stage: T for all steps in HBM, a tensor map over it, a persistent grid.
+void setup_col_tma(acq_plan* P, int n_prns) {
+    const Geometry& g = P->g;
+    P->col_tma = nullptr;
+    if (g.path != 0 || !P->tile_fs || getenv_flag("ACQ_GENERIC_FFT") || getenv_flag("ACQ_NO_TMA")) return;
+    ColTmaFn fn = pick_col_tma(g.ndop);
+    if (!fn || (g.spc % 2) != 0) return;
+    const size_t tall = sizeof(float2) * (size_t)g.n_nc * n_prns * g.ndop * g.spc;
+    if (tall > (24ull << 30)) return;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return;
+    int H = 0;
+    std::vector<int32_t> dr(g.ndop);
+    for (int m = 0; m < g.n_nc; ++m) {
+        code_drift_shifts(g, *P->sys, P->desc.sampling_freq_hz, m, dr.data());
+        for (int v : dr) H = std::max(H, std::min(v, g.spc - v));
+    }
+    const int W = 16;
+    if (H > W) return;
+    int box = 1;
+    for (int d = 1; d <= 256 && d <= g.ndop; ++d)
+        if (g.ndop % d == 0) box = d;
+    const size_t smem = 2 * sizeof(float2) * (size_t)g.ndop * W + sizeof(float) * (size_t)g.ndop * (W + 2 * H) +
+                        sizeof(int) * (size_t)g.n_nc * g.ndop + 16 + 16;
+    if (smem > 200 * 1024) return;
+    P->Tall.ensure(tall);
+    cuuint64_t gdim[2] = {static_cast<cuuint64_t>(g.spc), static_cast<cuuint64_t>(g.n_nc) * n_prns * g.ndop};
+    cuuint64_t gstride[1] = {static_cast<cuuint64_t>(g.spc) * sizeof(float2)};
+    cuuint32_t bdim[2] = {static_cast<cuuint32_t>(W), static_cast<cuuint32_t>(box)};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&P->tmapT, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, P->Tall.p, gdim, gstride, bdim, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        P->Tall.reset();
+        return;
+    }
+    set_smem((const void*)fn, smem);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kThreads, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        P->Tall.reset();
+        return;
+    }
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device));
+    P->errflag.ensure(sizeof(int));
+    CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
+    P->col_tma = fn;
+    P->tmaW = W;
+    P->tmaBoxRows = box;
+    P->tmaBoxes = g.ndop / box;
+    P->tmaGrid = sms * per_sm;
+    P->tmaH = H;
+    P->smem_col_tma = smem;
+}
+
 void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
     const Geometry& g = P->g;
     CK(cudaSetDevice(P->device));
@@ -319,9 +413,16 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         P->col_fs = g.path == 0 ? pick_col_fs(g.ndop) : nullptr;
     }
     if (P->tile_fs) {
-        P->tileNF = std::max(1, std::min(g.nb, static_cast<int>(48 * 1024 / (sizeof(float2) * g.fft_size)) - 1));
+        // one round of pass-1 tasks per chunk: NF * N2 <= threads (N2 = fft_size / best_split_n1)
+        const int n1 = best_split_n1(g.fft_size), n2 = g.fft_size / std::max(1, n1);
+        P->tileThreads = 128;
+        P->tileNF = std::max(1, std::min(g.nb, P->tileThreads / std::max(1, n2)));
+        if (const char* e = std::getenv("ACQ_TILE_THREADS")) P->tileThreads = std::max(32, std::min(256, std::atoi(e)));
         if (const char* e = std::getenv("ACQ_TILE_NF")) P->tileNF = std::max(1, std::min(g.nb, std::atoi(e)));
-        P->smem_tile_fs = sizeof(float2) * g.fft_size * (1 + P->tileNF);
+        // stagger neighbouring FFT buffers by 9 float2 (18 banks) so warps spanning two FFTs don't conflict
+        P->tileFS = g.fft_size + ((9 - (g.fft_size % 16) + 16) % 16);
+        if (const char* e = std::getenv("ACQ_TILE_PAD")) P->tileFS = g.fft_size + std::atoi(e);
+        P->smem_tile_fs = sizeof(float2) * (g.fft_size + (size_t)P->tileFS * P->tileNF);
         set_smem((const void*)P->tile_fs, P->smem_tile_fs);
     }
     if (P->col_fs) {
@@ -332,6 +433,7 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     }
     P->nct = (g.spc_eff + kStatsCols - 1) / kStatsCols;
     setup_fused(P);
+    setup_col_tma(P, n_prns);
 
     // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
     std::vector<int8_t> h_codes(static_cast<size_t>(n_prns) * g.spc);
@@ -476,13 +578,36 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
         t_end(P);
         ++L;
     }
-    for (int m = 0; m < (use_fused ? 0 : g.n_nc); ++m) {
+    const bool use_tma = !use_fused && P->col_tma != nullptr;
+    if (use_tma) {
+        // coherent tiles of every step in one launch, then the TMA-staged column stage
+        const int nprn = static_cast<int>(P->prns.size());
+        t_begin(P, ACQ_KERNEL_TILE);
+        P->tile_fs<<<dim3(G, n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
+            P->S.as<float2>(), P->conj.as<float2>(), P->slots.as<int>(), G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF,
+            inv_F, P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
+        t_end(P);
+        ++L;
+        if (P->tmaH > 0)
+            CK(cudaMemsetAsync(P->accb.p, 0, sizeof(float) * (size_t)n * g.ndop * g.spc_eff, st));
+        ColTmaParams cp{};
+        cp.spc = g.spc; cp.spc_eff = g.spc_eff; cp.n_nc = g.n_nc; cp.W = P->tmaW; cp.halo = P->tmaH;
+        cp.box_rows = P->tmaBoxRows; cp.n_boxes = P->tmaBoxes; cp.n_cblk = (g.spc + P->tmaW - 1) / P->tmaW;
+        cp.n_items = n * cp.n_cblk; cp.rows_per_step = nprn * g.ndop;
+        cp.twD = P->fftD.tw; cp.drift = P->drift.as<int>(); cp.acc = P->accb.as<float>(); cp.err = P->errflag.as<int>();
+        const int grid = std::max(1, std::min(P->tmaGrid, cp.n_items));
+        t_begin(P, ACQ_KERNEL_COLUMN);
+        P->col_tma<<<grid, kThreads, P->smem_col_tma, st>>>(P->tmapT, cp);
+        t_end(P);
+        ++L;
+    }
+    for (int m = 0; m < ((use_fused || use_tma) ? 0 : g.n_nc); ++m) {
         const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_size;
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
-            P->tile_fs<<<dim3(G, n), kThreads, P->smem_tile_fs, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G,
-                                                                     g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF, inv_F,
-                                                                     P->T.as<float2>());
+            P->tile_fs<<<dim3(G, n), P->tileThreads, P->smem_tile_fs, st>>>(
+                Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF, inv_F,
+                P->T.as<float2>(), 0, P->tileFS);
         else
             k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb,
                                                                g.bs, g.spc, P->fftF, P->tileB, inv_F, P->T.as<float2>());
@@ -568,6 +693,15 @@ void fetch(acq_plan* P, acq_result* results, float* power_bins) {
                            cudaMemcpyDeviceToHost, P->stream));
     CK(cudaStreamSynchronize(P->stream));
     t_collect(P);
+    if (P->errflag.p) {
+        int e = 0;
+        CK(cudaMemcpy(&e, P->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e != 0) {
+            CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
+            throw AcqError(ACQ_ERR_TIMEOUT, "a bounded wait for a TMA tile gave up (device error " +
+                                                std::to_string(e) + ")");
+        }
+    }
 }
 
 template <class F>
@@ -670,7 +804,7 @@ int acq_plan_destroy(acq_plan* P) {
     if (P->stream) cudaStreamSynchronize(P->stream);
     for (DevBuf* b : {&P->twF, &P->twD, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
                       &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
-                      &P->res, &P->slots, &P->prn_ids})
+                      &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag})
         b->reset();
     for (cudaEvent_t e : P->ev_start) cudaEventDestroy(e);
     for (cudaEvent_t e : P->ev_stop) cudaEventDestroy(e);

@@ -216,3 +216,17 @@ def test_power_bins_cached_buffer_reused():
     cached = plan.result_buffers[0]
     r2 = A.acquire_b(plan, sig, [1, 2], store_power_bins=True)
     assert plan.result_buffers[0] is cached and np.array_equal(r2[0].power_bins, cached)
+
+
+def test_tma_and_per_step_column_paths_agree(monkeypatch):
+    # The simple path runs either as one TMA-staged column launch over all steps or per step.
+    a_sys = A.GPSL1CA()
+    sats = [synth.Satellite(12, 40.0, 4800.0, 900.1)]
+    x = synth.to_ci16(synth.synth(a_sys, 5e6, 8 * 10 * 5000, sats, 5))
+    kw = dict(min_doppler_coverage=5000, num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=8)
+    ra = A.acquire_b(A.plan_acquire(a_sys, 5e6, [12, 13], **kw), x, [12, 13], store_power_bins=True)
+    monkeypatch.setenv("ACQ_NO_TMA", "1")
+    rb = A.acquire_b(A.plan_acquire(a_sys, 5e6, [12, 13], **kw), x, [12, 13], store_power_bins=True)
+    for a, b in zip(ra, rb):
+        assert (a.peak_doppler_bin, a.peak_code_bin) == (b.peak_doppler_bin, b.peak_code_bin)
+        assert np.abs(a.power_bins - b.power_bins).max() <= 1e-5 * b.power_bins.max()
