@@ -180,7 +180,9 @@ __device__ void fft_block(float2*& src, float2*& dst, const FftDesc& d, int B, i
 constexpr int kRegTwMax = 64;  // register-FFT sizes 2..64 have constant twiddle tables
 __host__ __device__ constexpr int reg_tw_offset(int n) { return (n - 1) * n / 2 - 1; }  // sum_{k=2}^{n-1} k
 constexpr int kRegTwEntries = reg_tw_offset(kRegTwMax + 1);
-__constant__ float2 c_regtw[kRegTwEntries];  // W_n^e = exp(-2 pi i e / n), filled by the host
+// One copy per translation unit (no relocatable device code): every unit that instantiates
+// register FFTs uploads it through its own acq_inst_*_upload_twiddles().
+static __constant__ float2 c_regtw[kRegTwEntries];  // W_n^e = exp(-2 pi i e / n)
 
 __host__ __device__ constexpr int first_factor(int n) {
     return n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : n % 7 == 0 ? 7 : n;

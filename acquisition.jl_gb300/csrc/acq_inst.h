@@ -1,0 +1,38 @@
+// acq_inst.h — the specialised-kernel dispatch tables. Each acq_inst_*.cu translation unit
+// instantiates one family of size-specialised kernels (compiled in parallel) and exports a
+// picker returning the kernel for a size (nullptr when that size has no specialisation) plus
+// the upload of its own copy of the register-FFT twiddle table.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "acq_kernels_fs.cuh"
+
+namespace acq {
+
+using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float,
+                          float2*, int64_t, int);
+using FusedFn = void (*)(FusedParams);
+using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, int, float*, int);
+using ColTmaFn = void (*)(const CUtensorMap, ColTmaParams);
+using SignFsFn = void (*)(const float2*, int, int, const float2*, const float*, int, int, int, int, int, const int*,
+                          const int*, int, float*, uint16_t*, int);
+using RotFsFn = void (*)(const float2*, int, int, const float2*, const float*, int, int, int, int, int, int, int, int,
+                         const int*, const int*, int, float*, uint16_t*, int);
+
+TileFsFn pick_tile_fs(int fft_size);
+FusedFn pick_fused(int fft_size, int ndop);
+ColFsFn pick_col_fs(int ndop);
+ColTmaFn pick_col_tma(int ndop);
+SignFsFn pick_sign_fs(int ndop);
+RotFsFn pick_rot_fs(int ndop);
+
+}  // namespace acq
+
+cudaError_t acq_inst_tile_upload_twiddles(const float2* host, size_t n);
+cudaError_t acq_inst_col_upload_twiddles(const float2* host, size_t n);
+cudaError_t acq_inst_sign_upload_twiddles(const float2* host, size_t n);

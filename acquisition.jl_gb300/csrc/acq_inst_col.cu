@@ -1,0 +1,33 @@
+// acq_inst_col.cu — simple-path Doppler column kernels (per step and TMA-staged) for hot ndop.
+#include "acq_inst.h"
+
+namespace acq {
+
+#define ACQ_COL_CASE(N) \
+    case N: return &k_col_simple_fs<best_split_n1(N), N / best_split_n1(N)>;
+#define ACQ_COLTMA_CASE(N) \
+    case N: return &k_col_tma<best_split_n1(N), N / best_split_n1(N)>;
+
+ColFsFn pick_col_fs(int ndop) {
+    switch (ndop) {
+        ACQ_COL_CASE(16) ACQ_COL_CASE(20) ACQ_COL_CASE(32) ACQ_COL_CASE(40) ACQ_COL_CASE(64) ACQ_COL_CASE(75)
+        ACQ_COL_CASE(100) ACQ_COL_CASE(160) ACQ_COL_CASE(200) ACQ_COL_CASE(240) ACQ_COL_CASE(320) ACQ_COL_CASE(400)
+        ACQ_COL_CASE(500) ACQ_COL_CASE(640) ACQ_COL_CASE(800) ACQ_COL_CASE(1280)
+        default: return nullptr;
+    }
+}
+
+ColTmaFn pick_col_tma(int ndop) {
+    switch (ndop) {
+        ACQ_COLTMA_CASE(16) ACQ_COLTMA_CASE(20) ACQ_COLTMA_CASE(32) ACQ_COLTMA_CASE(40) ACQ_COLTMA_CASE(64)
+        ACQ_COLTMA_CASE(75) ACQ_COLTMA_CASE(100) ACQ_COLTMA_CASE(160) ACQ_COLTMA_CASE(200) ACQ_COLTMA_CASE(240)
+        ACQ_COLTMA_CASE(320) ACQ_COLTMA_CASE(400) ACQ_COLTMA_CASE(500)
+        default: return nullptr;
+    }
+}
+
+}  // namespace acq
+
+cudaError_t acq_inst_col_upload_twiddles(const float2* host, size_t n) {
+    return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
+}

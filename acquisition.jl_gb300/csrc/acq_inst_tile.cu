@@ -1,0 +1,32 @@
+// acq_inst_tile.cu — coherent-tile and fused cluster kernels for the hot fft sizes.
+#include "acq_inst.h"
+
+namespace acq {
+
+#define ACQ_TILE_CASE(F) \
+    case F: return &k_tile_fs<best_split_n1(F), F / best_split_n1(F)>;
+
+TileFsFn pick_tile_fs(int F) {
+    switch (F) {
+        ACQ_TILE_CASE(128) ACQ_TILE_CASE(256) ACQ_TILE_CASE(500) ACQ_TILE_CASE(1000) ACQ_TILE_CASE(1250)
+        ACQ_TILE_CASE(1280) ACQ_TILE_CASE(1600) ACQ_TILE_CASE(2500)
+        default: return nullptr;
+    }
+}
+
+#define ACQ_FUSED_CASE(F, D) \
+    if (fft == F && ndop == D)   \
+        return &k_fused_simple<best_split_n1(F), F / best_split_n1(F), best_split_n1(D), D / best_split_n1(D)>;
+
+FusedFn pick_fused(int fft, int ndop) {
+    ACQ_FUSED_CASE(500, 200) ACQ_FUSED_CASE(500, 16) ACQ_FUSED_CASE(500, 20) ACQ_FUSED_CASE(256, 16)
+    ACQ_FUSED_CASE(256, 32) ACQ_FUSED_CASE(128, 32) ACQ_FUSED_CASE(1280, 75) ACQ_FUSED_CASE(2500, 20)
+    ACQ_FUSED_CASE(1250, 320) ACQ_FUSED_CASE(1250, 16) ACQ_FUSED_CASE(500, 40) ACQ_FUSED_CASE(500, 400)
+    return nullptr;
+}
+
+}  // namespace acq
+
+cudaError_t acq_inst_tile_upload_twiddles(const float2* host, size_t n) {
+    return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
+}

@@ -2,11 +2,10 @@
 // it replaces (paths inside JuliaGNSS/Acquisition.jl v2.6.4).
 #pragma once
 
-#include <cooperative_groups.h>
-#include <cuda.h>
 #include <cstdint>
 
 #include "acq_fft.cuh"
+#include "acq_kernels_fs.cuh"
 #include "acqgb300.h"
 
 namespace acq {
@@ -171,440 +170,6 @@ __global__ void k_col_simple(const float2* __restrict__ T, int ndop, int spc, in
         if (dc >= spc) dc -= spc;
         float* cell = ap + static_cast<int64_t>(row) * spc_eff + dc;
         *cell = first ? p : *cell + p;
-    }
-}
-
-// ------------------------------------------------------------------ specialised hot sizes
-// Coherent tile with the two-pass register FFT (F = N1 * N2): same mathematics as k_tile,
-// NF inverse FFTs per round; pass 1 forms S_g .* C*_m on the fly, pass 2 writes the first bs
-// lags of each row straight to the tile.
-template <int N1, int N2>
-__global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, const float2* __restrict__ C,
-                                                 const int* __restrict__ slots, int G, int nb, int bs, int spc,
-                                                 const float2* __restrict__ twF, int NF, float inv_F,
-                                                 float2* __restrict__ T, int64_t t_step_stride, int FS) {
-    constexpr int F = N1 * N2;
-    extern __shared__ float2 sm[];
-    float2* sg = sm;
-    float2* buf = sm + F;   // nf buffers of stride FS >= F (padding staggers the banks of neighbouring FFTs)
-    const int g = blockIdx.x;
-    const int pi = blockIdx.y;
-    const int slot = slots[pi];
-    const int k = g % nb;
-    const float2* Sg = S + (static_cast<int64_t>(blockIdx.z) * G + g) * F;
-    for (int t = threadIdx.x; t < F; t += blockDim.x) sg[t] = Sg[t];
-    __syncthreads();
-    float2* trow = T + blockIdx.z * t_step_stride + (static_cast<int64_t>(pi) * G + g) * spc;
-    for (int m0 = 0; m0 < nb; m0 += NF) {
-        const int nf = min(NF, nb - m0);
-        for (int task = threadIdx.x; task < nf * N2; task += blockDim.x) {
-            const int f = task / N2, n2 = task - f * N2;
-            const float2* Cm = C + (static_cast<int64_t>(slot) * nb + m0 + f) * F;
-            float2* x = buf + f * FS;
-            float2 v[N1];
-#pragma unroll
-            for (int n1 = 0; n1 < N1; ++n1) {
-                const int n = n2 + N2 * n1;
-                v[n1] = c_mul(sg[n], __ldg(Cm + n));
-            }
-            RegFFT<N1, true>::run(v);
-            static_for<0, N1>([&](auto kc) {
-                constexpr int k1 = decltype(kc)::value;
-                constexpr int pr = reg_perm(N1, k1);
-                float2 y = v[pr];
-                if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(twF, n2 * k1));
-                x[n2 + N2 * k1] = y;
-            });
-        }
-        __syncthreads();
-        for (int task = threadIdx.x; task < nf * N1; task += blockDim.x) {
-            const int f = task / N1, k1 = task - f * N1;
-            const float2* x = buf + f * FS;
-            float2 v[N2];
-#pragma unroll
-            for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[N2 * k1 + n2];
-            RegFFT<N2, true>::run(v);
-            int r = m0 + f - k;
-            if (r < 0) r += nb;
-            float2* dst = trow + r * bs;
-            static_for<0, N2>([&](auto kc) {
-                constexpr int k2 = decltype(kc)::value;
-                constexpr int pr = reg_perm(N2, k2);
-                const int j = k1 + N1 * k2;
-                if (j < bs) {
-                    const float2 y = v[pr];
-                    dst[j] = make_float2(y.x * inv_F, y.y * inv_F);
-                }
-            });
-        }
-        __syncthreads();
-    }
-}
-
-// Simple column stage with the two-pass register FFT (ndop = N1 * N2): in place in shared
-// memory, |X|^2, fftshift and the destination-row drift scatter fused into pass 2.
-template <int N1, int N2>
-__global__ void __launch_bounds__(256) k_col_simple_fs(const float2* __restrict__ T, int spc, int W,
-                                                       const float2* __restrict__ twD, const int* __restrict__ drift,
-                                                       int first, int has_drift, float* __restrict__ acc, int spc_eff) {
-    constexpr int ND = N1 * N2;
-    extern __shared__ float2 sm[];
-    int* dr = reinterpret_cast<int*>(sm + ND * W);
-    const int pi = blockIdx.y;
-    const int c0 = blockIdx.x * W;
-    const int wv = min(W, spc - c0);
-    const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
-    for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
-        const int e = w / W, t = w - e * W;
-        sm[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
-    }
-    for (int i = threadIdx.x; i < ND; i += blockDim.x) dr[i] = has_drift ? drift[i] : 0;
-    __syncthreads();
-    for (int task = threadIdx.x; task < N2 * W; task += blockDim.x) {
-        const int n2 = task / W, t = task - n2 * W;
-        fourstep_pass1<N1, N2, false>(sm + t, W, n2, twD);
-    }
-    __syncthreads();
-    constexpr int half = ND / 2;
-    float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
-    for (int task = threadIdx.x; task < N1 * W; task += blockDim.x) {
-        const int k1 = task / W, t = task - k1 * W;
-        if (t >= wv) continue;
-        const int c = c0 + t;
-        float2 v[N2];
-#pragma unroll
-        for (int n2 = 0; n2 < N2; ++n2) v[n2] = sm[(N2 * k1 + n2) * W + t];
-        RegFFT<N2, false>::run(v);
-        // power in natural order, then the accumulator cells: loads batched ahead of the stores
-        float p[N2];
-        int64_t idx[N2];
-        static_for<0, N2>([&](auto kc) {
-            constexpr int k2 = decltype(kc)::value;
-            constexpr int pr = reg_perm(N2, k2);
-            const float2 x = v[pr];
-            p[k2] = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
-            int row = k1 + N1 * k2 + half;
-            if (row >= ND) row -= ND;
-            int dc = c + dr[row];
-            if (dc >= spc) dc -= spc;
-            idx[k2] = static_cast<int64_t>(row) * spc_eff + dc;
-        });
-        if (first) {
-#pragma unroll
-            for (int k2 = 0; k2 < N2; ++k2) ap[idx[k2]] = p[k2];
-        } else {
-            float old[N2];
-#pragma unroll
-            for (int k2 = 0; k2 < N2; ++k2) old[k2] = ap[idx[k2]];
-#pragma unroll
-            for (int k2 = 0; k2 < N2; ++k2) ap[idx[k2]] = __fadd_rn(old[k2], p[k2]);
-        }
-    }
-}
-
-// ------------------------------------------------------------------ TMA-staged column stage
-// mbarrier / bulk-tensor helpers (PTX ISA 8.x).
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-            "r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
-
-// Bounded wait on an mbarrier phase: gives up after kWaitLimit polls, records `code` in *err.
-constexpr uint32_t kWaitLimit = 1u << 24;
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int code) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    atomicExch(err, code);
-    return false;
-}
-
-struct ColTmaParams {
-    int spc, spc_eff, n_nc, W, halo, box_rows, n_boxes, n_items, n_cblk, rows_per_step;
-    const float2* twD;
-    const int* drift;      // (n_nc, ndop) in [0, spc)
-    float* acc;            // (n_req, ndop, spc_eff)
-    int* err;
-};
-
-// Persistent column stage for all accumulation steps of the simple path. Work item = (requested
-// PRN, block of W code-phase columns); for every step the (ndop x W) tile of the coherent
-// matrix arrives by TMA into one of two shared buffers while the other is transformed. The
-// Doppler FFT (four-step, in place), |X|^2, fftshift and the destination-row drift scatter go
-// into a shared accumulator with an H-column halo; it is written once per work item (interior
-// stored, halo/edge atomically added to the zeroed accumulator). Replaces the per-step column
-// kernel and its accumulator read-modify-write (src/noncoherent_integration.jl:482-592).
-template <int N1, int N2>
-__global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtensorMap tmap, ColTmaParams p) {
-    constexpr int ND = N1 * N2;
-    const int W = p.W, H = p.halo, AW = p.W + 2 * p.halo;
-    extern __shared__ __align__(128) unsigned char smraw[];
-    float2* buf[2];
-    buf[0] = reinterpret_cast<float2*>(smraw);
-    buf[1] = buf[0] + ND * W;
-    float* accs = reinterpret_cast<float*>(buf[1] + ND * W);
-    int* drs = reinterpret_cast<int*>(accs + ND * AW);
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smraw) + ((2 * ND * W * 8 + ND * AW * 4 + p.n_nc * ND * 4 + 15) / 8);
-    const uint32_t tile_bytes = static_cast<uint32_t>(ND) * W * 8;
-    if (threadIdx.x == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
-        mbar_fence_init();
-    }
-    for (int i = threadIdx.x; i < p.n_nc * ND; i += blockDim.x) {
-        int sh = p.drift[i];
-        if (sh > p.spc / 2) sh -= p.spc;
-        drs[i] = sh;
-    }
-    for (int i = threadIdx.x; i < ND * AW; i += blockDim.x) accs[i] = 0.f;
-    __syncthreads();
-    // this CTA's tile sequence: k -> (item = blockIdx.x + (k / n_nc) * gridDim.x, step = k % n_nc)
-    const int my_items = p.n_items > static_cast<int>(blockIdx.x)
-                             ? (p.n_items - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
-                             : 0;
-    const int K = my_items * p.n_nc;
-    auto issue = [&](int k) {
-        const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
-        const int m = k % p.n_nc;
-        const int pi = item / p.n_cblk, cb = item - pi * p.n_cblk;
-        const int b = k & 1;
-        fence_proxy_async();
-        mbar_expect_tx(&mbar[b], tile_bytes);
-        const int row0 = m * p.rows_per_step + pi * ND;
-        for (int rb = 0; rb < p.n_boxes; ++rb)
-            tma_load_2d(buf[b] + rb * p.box_rows * W, &tmap, cb * W, row0 + rb * p.box_rows, &mbar[b]);
-    };
-    uint32_t phase[2] = {0u, 0u};
-    if (threadIdx.x == 0 && K > 0) issue(0);
-    constexpr int half = ND / 2;
-    for (int k = 0; k < K; ++k) {
-        const int b = k & 1;
-        if (threadIdx.x == 0 && k + 1 < K) issue(k + 1);
-        if (!mbar_wait_bounded(&mbar[b], phase[b], p.err, 1)) {
-            // give the copies in flight a bounded chance to land, then leave
-            mbar_wait_bounded(&mbar[b ^ 1], phase[b ^ 1], p.err, 1);
-            return;
-        }
-        phase[b] ^= 1u;
-        const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
-        const int m = k % p.n_nc;
-        const int pi = item / p.n_cblk, cb = item - pi * p.n_cblk;
-        const int c0 = cb * W;
-        const int wv = min(W, p.spc - c0);
-        float2* tl = buf[b];
-        for (int task = threadIdx.x; task < N2 * W; task += blockDim.x) {
-            const int n2 = task / W, t = task - n2 * W;
-            fourstep_pass1<N1, N2, false>(tl + t, W, n2, p.twD);
-        }
-        __syncthreads();
-        const int* dm = drs + m * ND;
-        for (int task = threadIdx.x; task < N1 * W; task += blockDim.x) {
-            const int k1 = task / W, t = task - k1 * W;
-            if (t >= wv) continue;
-            float2 v[N2];
-#pragma unroll
-            for (int n2 = 0; n2 < N2; ++n2) v[n2] = tl[(N2 * k1 + n2) * W + t];
-            RegFFT<N2, false>::run(v);
-            static_for<0, N2>([&](auto kc) {
-                constexpr int k2 = decltype(kc)::value;
-                constexpr int pr = reg_perm(N2, k2);
-                const float2 xv = v[pr];
-                const float pw = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
-                int row = k1 + N1 * k2 + half;
-                if (row >= ND) row -= ND;
-                float* cell = accs + row * AW + H + t + dm[row];
-                *cell = __fadd_rn(*cell, pw);
-            });
-        }
-        __syncthreads();
-        if (m == p.n_nc - 1) {
-            float* ap = p.acc + static_cast<int64_t>(pi) * ND * p.spc_eff;
-            const int span = wv + 2 * H;
-            for (int i = threadIdx.x; i < ND * span; i += blockDim.x) {
-                const int row = i / span;
-                const int lc = -H + (i - row * span);
-                float* src = accs + row * AW + H + lc;
-                const float v = *src;
-                *src = 0.f;
-                int c = c0 + lc;
-                if (c < 0) c += p.spc;
-                if (c >= p.spc) c -= p.spc;
-                float* cell = ap + static_cast<int64_t>(row) * p.spc_eff + c;
-                if (H == 0 || (lc >= H && lc < wv - H)) *cell = v;
-                else if (v != 0.f) atomicAdd(cell, v);
-            }
-            __syncthreads();
-        }
-    }
-}
-
-// ------------------------------------------------------------------ fused simple path
-// One thread-block cluster of CL CTAs per (requested PRN, column block r) runs every
-// accumulation step of the simple path without touching HBM in between:
-//   1. CTA q inverse-FFTs its rows g in [q*RPC, (q+1)*RPC) (F = N1F*N2F, S_g .* C*_{(k+r) mod nb})
-//      and stores lag j of row g into the shared memory of the CTA that owns column j
-//      (distributed shared memory, columns [q*CPC, (q+1)*CPC) belong to CTA q);
-//   2. after a cluster barrier each CTA runs the Doppler FFT (ndop = N1D*N2D) down its CPC
-//      columns and adds |X|^2 (fftshift, destination-row drift) into a shared-memory
-//      accumulator with an H-column halo on each side;
-//   3. after the last step interior columns are stored, halo/edge columns are atomically added
-//      to the (zeroed) global accumulator.
-// Same mathematics as k_tile + k_col_simple_fs; the per-cell step order of the sums is kept.
-struct FusedParams {
-    int G, nb, bs, spc, spc_eff, n_nc, rpc, cpc, nf, halo;
-    float inv_F;
-    const float2* S;       // (n_nc, G, F)
-    const float2* C;       // (slots, nb, F)
-    const int* slots;
-    const float2* twF;
-    const float2* twD;
-    const int* drift;      // (n_nc, ndop) in [0, spc)
-    float* acc;            // (n_req, ndop, spc_eff)
-};
-
-template <int N1F, int N2F, int N1D, int N2D>
-__global__ void __launch_bounds__(256) k_fused_simple(FusedParams fp) {
-    namespace cg = cooperative_groups;
-    constexpr int F = N1F * N2F;
-    constexpr int ND = N1D * N2D;
-    constexpr int NW = 8;                       // warps per CTA (256 threads)
-    cg::cluster_group cluster = cg::this_cluster();
-    const int q = static_cast<int>(cluster.block_rank());
-    const int CL = static_cast<int>(cluster.num_blocks());
-    const int r = blockIdx.x / CL;
-    const int pi = blockIdx.y;
-    const int slot = fp.slots[pi];
-    const int CPC = fp.cpc, H = fp.halo, AW = fp.cpc + 2 * fp.halo;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    extern __shared__ float2 sm[];
-    float2* tile = sm;                                         // ND x CPC, written by every CTA of the cluster
-    float2* wbuf = tile + ND * CPC + wid * F;                  // this warp's FFT buffer (NW x F)
-    float* accl = reinterpret_cast<float*>(tile + ND * CPC + NW * F);   // ND x AW
-    int* dr = reinterpret_cast<int*>(accl + ND * AW);          // this step's signed drift per sorted row
-    const int g0 = q * fp.rpc, g1 = min(ND, g0 + fp.rpc);
-    const int j0 = q * CPC;
-    const int wv = max(0, min(CPC, fp.bs - j0));
-    const int cpw = (CPC + NW - 1) / NW;                       // Doppler columns per warp
-    for (int i = threadIdx.x; i < ND * AW; i += blockDim.x) accl[i] = 0.f;
-    cluster.sync();   // every CTA of the cluster is running before any remote store
-    constexpr int half = ND / 2;
-    for (int m = 0; m < fp.n_nc; ++m) {
-        const float2* Sm = fp.S + static_cast<int64_t>(m) * fp.G * F;
-        for (int i = threadIdx.x; i < ND; i += blockDim.x) {
-            int sh = fp.drift[m * ND + i];
-            if (sh > fp.spc / 2) sh -= fp.spc;       // signed drift, |sh| <= H
-            dr[i] = sh;
-        }
-        // ---- inverse FFTs: warp wid owns rows g0+wid, g0+wid+NW, ...; lags go to their owner CTA
-        for (int g = g0 + wid; g < g1; g += NW) {
-            const int cm = (g % fp.nb + r) % fp.nb;
-            const float2* Sg = Sm + static_cast<int64_t>(g) * F;
-            const float2* Cm = fp.C + (static_cast<int64_t>(slot) * fp.nb + cm) * F;
-            for (int n2 = lane; n2 < N2F; n2 += 32) {
-                float2 v[N1F];
-#pragma unroll
-                for (int n1 = 0; n1 < N1F; ++n1) {
-                    const int n = n2 + N2F * n1;
-                    v[n1] = c_mul(__ldg(Sg + n), __ldg(Cm + n));
-                }
-                RegFFT<N1F, true>::run(v);
-                static_for<0, N1F>([&](auto kc) {
-                    constexpr int k1 = decltype(kc)::value;
-                    constexpr int pr = reg_perm(N1F, k1);
-                    float2 y = v[pr];
-                    if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(fp.twF, n2 * k1));
-                    wbuf[n2 + N2F * k1] = y;
-                });
-            }
-            __syncwarp();
-            for (int k1 = lane; k1 < N1F; k1 += 32) {
-                float2 v[N2F];
-#pragma unroll
-                for (int n2 = 0; n2 < N2F; ++n2) v[n2] = wbuf[N2F * k1 + n2];
-                RegFFT<N2F, true>::run(v);
-                static_for<0, N2F>([&](auto kc) {
-                    constexpr int k2 = decltype(kc)::value;
-                    constexpr int pr = reg_perm(N2F, k2);
-                    const int j = k1 + N1F * k2;
-                    if (j < fp.bs) {
-                        const int owner = j / CPC;
-                        float2* dst = cluster.map_shared_rank(tile, owner);
-                        const float2 y = v[pr];
-                        dst[g * CPC + (j - owner * CPC)] = make_float2(y.x * fp.inv_F, y.y * fp.inv_F);
-                    }
-                });
-            }
-            __syncwarp();
-        }
-        cluster.sync();
-        // ---- Doppler FFT: warp wid owns columns [wid*cpw, (wid+1)*cpw); each destination cell gets
-        // exactly one contribution per step (the drift scatter is a bijection per row)
-        const int t0 = wid * cpw, t1 = min(wv, t0 + cpw);
-        const int ncw = max(0, t1 - t0);
-        for (int task = lane; task < N2D * ncw; task += 32) {
-            const int n2 = task / ncw, t = t0 + (task - n2 * ncw);
-            fourstep_pass1<N1D, N2D, false>(tile + t, CPC, n2, fp.twD);
-        }
-        __syncwarp();
-        for (int task = lane; task < N1D * ncw; task += 32) {
-            const int k1 = task / ncw, t = t0 + (task - k1 * ncw);
-            float2 v[N2D];
-#pragma unroll
-            for (int n2 = 0; n2 < N2D; ++n2) v[n2] = tile[(N2D * k1 + n2) * CPC + t];
-            RegFFT<N2D, false>::run(v);
-            static_for<0, N2D>([&](auto kc) {
-                constexpr int k2 = decltype(kc)::value;
-                constexpr int pr = reg_perm(N2D, k2);
-                const float2 xv = v[pr];
-                const float p = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
-                int row = k1 + N1D * k2 + half;
-                if (row >= ND) row -= ND;
-                float* cell = accl + row * AW + H + t + dr[row];
-                *cell = __fadd_rn(*cell, p);
-            });
-        }
-        cluster.sync();   // every CTA is done with its tile (and dr) before the next step overwrites it
-    }
-    // ---- write back: interior columns are owned, halo/edge columns are shared with neighbours
-    float* ap = fp.acc + static_cast<int64_t>(pi) * ND * fp.spc_eff;
-    const int cbase = r * fp.bs + j0;
-    const int lo = -H, hi = wv + H;
-    const int span = hi - lo;
-    for (int i = threadIdx.x; i < ND * span; i += blockDim.x) {
-        const int row = i / span;
-        const int lc = lo + (i - row * span);
-        const float v = accl[row * AW + H + lc];
-        int c = cbase + lc;
-        if (c < 0) c += fp.spc;
-        if (c >= fp.spc) c -= fp.spc;
-        float* cell = ap + static_cast<int64_t>(row) * fp.spc_eff + c;
-        if (H == 0 || (lc >= H && lc < wv - H)) *cell = v;
-        else if (v != 0.f) atomicAdd(cell, v);
     }
 }
 

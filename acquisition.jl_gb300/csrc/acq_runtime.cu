@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "acq_host.h"
+#include "acq_inst.h"
 #include "acq_kernels.cuh"
 
 using namespace acq;
@@ -93,22 +94,9 @@ void upload_reg_twiddles() {
             double a = -2.0 * M_PI * static_cast<double>(e) / static_cast<double>(n);
             h[reg_tw_offset(n) + e] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
         }
-    CK(cudaMemcpyToSymbol(c_regtw, h.data(), sizeof(float2) * h.size()));
-}
-
-using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float,
-                          float2*, int64_t, int);
-using ColTmaFn = void (*)(const CUtensorMap, ColTmaParams);
-
-#define ACQ_COLTMA_CASE(N) \
-    case N: return &k_col_tma<best_split_n1(N), N / best_split_n1(N)>;
-
-ColTmaFn pick_col_tma(int ndop) {
-    switch (ndop) {
-        ACQ_COLTMA_CASE(16) ACQ_COLTMA_CASE(20) ACQ_COLTMA_CASE(32) ACQ_COLTMA_CASE(40) ACQ_COLTMA_CASE(64)
-        ACQ_COLTMA_CASE(75) ACQ_COLTMA_CASE(100) ACQ_COLTMA_CASE(160) ACQ_COLTMA_CASE(200) ACQ_COLTMA_CASE(240)
-        ACQ_COLTMA_CASE(320) ACQ_COLTMA_CASE(400) ACQ_COLTMA_CASE(500)
-        default: return nullptr;
+    for (auto up : {acq_inst_tile_upload_twiddles, acq_inst_col_upload_twiddles, acq_inst_sign_upload_twiddles}) {
+        cudaError_t e = up(h.data(), h.size());
+        if (e != cudaSuccess) throw CudaError(std::string("twiddle upload: ") + cudaGetErrorString(e));
     }
 }
 
@@ -126,43 +114,6 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     }
     return fn;
 }
-using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, int, float*, int);
-
-#define ACQ_TILE_CASE(F) \
-    case F: return &k_tile_fs<best_split_n1(F), F / best_split_n1(F)>;
-#define ACQ_COL_CASE(N) \
-    case N: return &k_col_simple_fs<best_split_n1(N), N / best_split_n1(N)>;
-
-TileFsFn pick_tile_fs(int F) {
-    switch (F) {
-        ACQ_TILE_CASE(128) ACQ_TILE_CASE(256) ACQ_TILE_CASE(500) ACQ_TILE_CASE(1000) ACQ_TILE_CASE(1250)
-        ACQ_TILE_CASE(1280) ACQ_TILE_CASE(1600) ACQ_TILE_CASE(2500)
-        default: return nullptr;
-    }
-}
-
-ColFsFn pick_col_fs(int ndop) {
-    switch (ndop) {
-        ACQ_COL_CASE(16) ACQ_COL_CASE(20) ACQ_COL_CASE(32) ACQ_COL_CASE(40) ACQ_COL_CASE(64) ACQ_COL_CASE(75)
-        ACQ_COL_CASE(100) ACQ_COL_CASE(160) ACQ_COL_CASE(200) ACQ_COL_CASE(240) ACQ_COL_CASE(320) ACQ_COL_CASE(400)
-        ACQ_COL_CASE(500) ACQ_COL_CASE(640) ACQ_COL_CASE(800) ACQ_COL_CASE(1280)
-        default: return nullptr;
-    }
-}
-
-using FusedFn = void (*)(FusedParams);
-
-#define ACQ_FUSED_CASE(F, D)                                                                  \
-    if (fft == F && ndop == D)                                                                \
-        return &k_fused_simple<best_split_n1(F), F / best_split_n1(F), best_split_n1(D), D / best_split_n1(D)>;
-
-FusedFn pick_fused(int fft, int ndop) {
-    ACQ_FUSED_CASE(500, 200) ACQ_FUSED_CASE(500, 16) ACQ_FUSED_CASE(500, 20) ACQ_FUSED_CASE(256, 16)
-    ACQ_FUSED_CASE(256, 32) ACQ_FUSED_CASE(128, 32) ACQ_FUSED_CASE(1280, 75) ACQ_FUSED_CASE(2500, 20)
-    ACQ_FUSED_CASE(1250, 320) ACQ_FUSED_CASE(1250, 16) ACQ_FUSED_CASE(500, 40) ACQ_FUSED_CASE(500, 400)
-    return nullptr;
-}
-
 int pow2_floor(int x) {
     int p = 1;
     while (p * 2 <= x) p *= 2;
@@ -209,6 +160,11 @@ struct acq_plan {
     int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1;
     std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
+    // specialised sign / rotation stages
+    SignFsFn sign_fs = nullptr;
+    RotFsFn rot_fs = nullptr;
+    int Wsfs = 8;
+    size_t smem_sfs = 0;
     // TMA-staged column stage over all steps (simple path)
     ColTmaFn col_tma = nullptr;
     CUtensorMap tmapT{};
@@ -425,6 +381,19 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         P->smem_tile_fs = sizeof(float2) * (g.fft_size + (size_t)P->tileFS * P->tileNF);
         set_smem((const void*)P->tile_fs, P->smem_tile_fs);
     }
+    if (!getenv_flag("ACQ_GENERIC_FFT") && (g.ndop % 2) == 0) {
+        if (g.path == 1) P->sign_fs = pick_sign_fs(g.ndop);
+        if (g.path == 2) P->rot_fs = pick_rot_fs(g.ndop);
+    }
+    if (P->sign_fs || P->rot_fs) {
+        const size_t per = 2 * 8 + 4 + 2;   // tile + work (float2), stage (float), winner (u16)
+        int W = 16;
+        while (W > 1 && per * (size_t)g.ndop * W + 4 * W + 16 > 110 * 1024) W /= 2;
+        P->Wsfs = W;
+        P->smem_sfs = per * (size_t)g.ndop * W + 4 * W + 16;
+        if (P->sign_fs) set_smem((const void*)P->sign_fs, P->smem_sfs);
+        if (P->rot_fs) set_smem((const void*)P->rot_fs, P->smem_sfs);
+    }
     if (P->col_fs) {
         P->Wfs = g.ndop <= 400 ? 32 : g.ndop <= 800 ? 16 : 8;
         if (const char* e = std::getenv("ACQ_COL_W")) P->Wfs = std::max(1, std::min(64, std::atoi(e)));
@@ -625,6 +594,18 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
             const int W = P->Wsimple;
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
+        } else if (g.path == 1 && P->sign_fs) {
+            const int W = P->Wsfs;
+            P->sign_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
+                P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
+                P->edge_step, P->slots.as<int>(), dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+        } else if (g.path == 2 && P->rot_fs) {
+            const int W = P->Wsfs;
+            const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            P->rot_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
+                P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), g.n_coh, g.nb, g.bs, g.R, P->combos,
+                g.n_be, P->edge_step, use_max, P->slots.as<int>(), dr, first, P->accb.as<float>(),
+                P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 1) {
             const int W = P->Wsign;
             k_col_sign<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(

@@ -36,22 +36,65 @@ for _p in (ROOT, os.path.join(ROOT, "acquisition.jl_gb300")):
 
 import numpy as np  # noqa: E402
 
-FS = 5e6
-N_COH, N_NC, COV = 10, 8, 5000.0
 PRNS = list(range(1, 33))
 SEED = 2024
-WORKLOAD = "gps_l1ca_5MHz_10msx8_pm5kHz_32prn_ci16"
+
+# Workloads of the reference's configurations (seeded synthetic recordings stand in for data).
+CONFIGS = {
+    # headline: GPS L1 C/A weak-signal search, 5 MHz, 10 ms x 8, +-5 kHz, CI16
+    "cfg2": dict(workload="gps_l1ca_5MHz_10msx8_pm5kHz_32prn_ci16", system="GPSL1CA", fs=5e6, n_coh=10, n_nc=8,
+                 n_be=1, cov=5000.0, quant="ci16", n_sats=4, cn0=(35.0, 42.0), dmax=5000.0, bit_period=0.02),
+    # CPU-runnable plain case: 4 MHz, 1 ms, +-7 kHz, CF32, PRN 1 at 45 dB-Hz
+    "cfg1": dict(workload="gps_l1ca_4MHz_1ms_pm7kHz_32prn_cf32", system="GPSL1CA", fs=4e6, n_coh=1, n_nc=1, n_be=1,
+                 cov=7000.0, quant=None, fixed=[(1, 45.0, 1234.0, 300.5)], bit_period=0.02),
+    # bit-edge / data-bit search: the same 80 ms as 40 ms x 2 (ndop 800, 2 data bits, 4 bit edges)
+    "cfg2b": dict(workload="gps_l1ca_5MHz_40msx2_pm5kHz_nbe4_32prn_ci16", system="GPSL1CA", fs=5e6, n_coh=40,
+                  n_nc=2, n_be=4, cov=5000.0, quant="ci16", n_sats=4, cn0=(35.0, 42.0), dmax=5000.0,
+                  bit_period=0.02),
+    # secondary-code rotation search: GPS L5I 20 MHz, 20 ms x 4, +-10 kHz, CI8 (3-bit)
+    "cfg4": dict(workload="gps_l5i_20MHz_20msx4_pm10kHz_32prn_ci8", system="GPSL5I", fs=20e6, n_coh=20, n_nc=4,
+                 n_be=1, cov=10000.0, quant="ci8", n_sats=6, cn0=(30.0, 45.0), dmax=10000.0, bit_period=0.01),
+}
+CFG = CONFIGS["cfg2"]
+FS, N_COH, N_NC, COV = CFG["fs"], CFG["n_coh"], CFG["n_nc"], CFG["cov"]
+WORKLOAD = CFG["workload"]
+
+
+def set_config(name):
+    global CFG, FS, N_COH, N_NC, COV, WORKLOAD
+    CFG = CONFIGS[name]
+    FS, N_COH, N_NC, COV, WORKLOAD = CFG["fs"], CFG["n_coh"], CFG["n_nc"], CFG["cov"], CFG["workload"]
+
+
+def system_of(cfg):
+    import acqgb300 as A
+    return {"GPSL1CA": A.GPSL1CA, "GPSL5I": A.GPSL5I, "GalileoE1B": A.GalileoE1B}[cfg["system"]]()
 
 
 def make_input():
-    import acqgb300 as A
     from acqgb300 import synth
+    sysm = system_of(CFG)
     rng = np.random.default_rng(SEED)
-    present = sorted(rng.choice(np.arange(1, 33), size=4, replace=False).tolist())
-    sats = synth.random_sats(rng, present, (35.0, 42.0), 5000.0, 1023.0, bit_period_s=0.02)
-    n = N_NC * N_COH * 5000
-    x = synth.synth(A.GPSL1CA(), FS, n, sats, SEED)
-    return synth.to_ci16(x), sats
+    if "fixed" in CFG:
+        sats = [synth.Satellite(p, c, d, cp) for (p, c, d, cp) in CFG["fixed"]]
+    else:
+        present = sorted(rng.choice(np.arange(1, 33), size=CFG["n_sats"], replace=False).tolist())
+        sats = synth.random_sats(rng, present, CFG["cn0"], CFG["dmax"], sysm.code_length,
+                                 bit_period_s=CFG["bit_period"])
+    spc = int(math.ceil(sysm.code_length / sysm.code_frequency * FS))
+    n = N_NC * N_COH * spc
+    x = synth.synth(sysm, FS, n, sats, SEED)
+    if CFG["quant"] == "ci16":
+        return synth.to_ci16(x), sats
+    if CFG["quant"] == "ci8":
+        return synth.to_ci8_3bit(x), sats
+    return x.astype(np.complex64), sats
+
+
+def as_complex64(sig):
+    if np.iscomplexobj(sig):
+        return sig.astype(np.complex64)
+    return (sig[:, 0].astype(np.float32) + 1j * sig[:, 1].astype(np.float32)).astype(np.complex64)
 
 
 def peaks():
@@ -113,13 +156,21 @@ class ClockSampler:
                 "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
 
 
-def cpu_port_time_per_prn(ci16, steps: int = 1):
-    """Time the oracle's FP32 restatement for one PRN through all accumulation steps."""
+def cpu_port_sample():
+    """(accumulation steps timed per sample, scale factor to one 32-PRN acquisition)."""
+    n_nc = min(N_NC, 1 if CFG["system"] == "GPSL5I" and N_COH > 1 else N_NC)
+    return n_nc, len(PRNS) * N_NC / n_nc
+
+
+def cpu_port_time_per_prn(sig, steps: int = 1):
+    """Time the oracle's FP32 restatement for one PRN (all steps, or one step of a rotation search)."""
     from oracle import acq_oracle as O
     from oracle import gnss_codes as G
-    sig = (ci16[:, 0].astype(np.float32) + 1j * ci16[:, 1].astype(np.float32)).astype(np.complex64)
-    plan = O.plan_acquire(G.GPSL1CA, FS, [1], min_doppler_coverage=COV, num_coherently_integrated_code_periods=N_COH,
-                          num_noncoherent_accumulations=N_NC, precision="f32")
+    n_nc, _ = cpu_port_sample()
+    sig = as_complex64(sig)
+    plan = O.plan_acquire(G.SYSTEMS[CFG["system"]], FS, [1], min_doppler_coverage=COV,
+                          num_coherently_integrated_code_periods=N_COH, bit_edge_search_steps=CFG["n_be"],
+                          num_noncoherent_accumulations=n_nc, precision="f32")
     times = []
     for _ in range(steps):
         t0 = time.perf_counter()
@@ -133,20 +184,20 @@ def run_reference(args):
     for _ in range(args.warmup):
         cpu_port_time_per_prn(ci16, 1)
     times = cpu_port_time_per_prn(ci16, args.steps)
-    per_acq = statistics.mean(times) * len(PRNS)
+    per_acq = statistics.mean(times) * cpu_port_sample()[1]
     value = 1.0 / per_acq
     cores = os.cpu_count()
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_acq * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "prns": 32, "samples": N_NC * N_COH * 5000},
+            "config": {"workload": WORKLOAD, "prns": 32, "samples": int(len(ci16))},
             "cpu_baseline": {"value": value, "unit": "acq/s", "cores": cores, "kind": "port",
-                             "sample": "1 PRN x 8 accumulation steps per step, extrapolated x32 PRNs; the Julia "
-                                       "reference is unavailable here, its algorithm runs as the oracle's FP32 "
-                                       "numpy/scipy restatement (scipy.fft workers=-1)"},
+                             "sample": f"1 PRN x {cpu_port_sample()[0]} accumulation step(s) per step, extrapolated to "
+                                       "32 PRNs x all steps; the Julia reference is unavailable here, its algorithm "
+                                       "runs as the oracle's FP32 numpy/scipy restatement (scipy.fft workers=-1)"},
             "e2e": {"value": value, "unit": "acq/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "msample_prn_per_s": value * 32 * N_NC * N_COH * 5000 / 1e6}
+            "msample_prn_per_s": value * 32 * len(ci16) / 1e6}
     print(json.dumps(line))
 
 
@@ -159,9 +210,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="plain", choices=["fused", "plain"],
                     help="kernel form of the headline measurement (the other form is reported beside it)")
-    ap.add_argument("--accumulations", type=int, default=N_NC,
-                    help="non-coherent accumulations (profiling cases only; the workload uses 8)")
+    ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS),
+                    help="workload (cfg2, the reference's weak-signal search, is the headline)")
+    ap.add_argument("--accumulations", type=int, default=None,
+                    help="non-coherent accumulations (profiling cases only; default: the workload's)")
     args = ap.parse_args()
+    set_config(args.config)
     args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -183,12 +237,17 @@ def main():
         dist.init_process_group("nccl")
 
     ci16, sats = make_input()
-    n_nc = args.accumulations
-    plan = A.plan_acquire(A.GPSL1CA(), FS, PRNS, min_doppler_coverage=COV, num_coherently_integrated_code_periods=N_COH,
+    n_nc = args.accumulations or N_NC
+    plan = A.plan_acquire(system_of(CFG), FS, PRNS, min_doppler_coverage=COV,
+                          num_coherently_integrated_code_periods=N_COH, bit_edge_search_steps=CFG["n_be"],
                           num_noncoherent_accumulations=n_nc, device=local_rank)
     main_form = plan.set_form(args.form)
     other_form = "plain" if main_form == "fused" else "fused"
-    host = torch.from_numpy(ci16).pin_memory()
+    if np.iscomplexobj(ci16):
+        host = torch.from_numpy(ci16.view(np.float32).reshape(-1, 2)).pin_memory()
+    else:
+        host = torch.from_numpy(ci16).pin_memory()
+    host_np = host.numpy()
     dev = host.to(f"cuda:{local_rank}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
     pstream = torch.cuda.ExternalStream(plan.stream_handle(), device=f"cuda:{local_rank}")
@@ -200,7 +259,7 @@ def main():
     # warm-up (device-resident and public API)
     for _ in range(args.warmup):
         A.acquire_device(plan, dev, PRNS)
-        A.acquire_b(plan, host.numpy(), PRNS)
+        A.acquire_b(plan, host_np, PRNS)
     res = A.acquire_device(plan, dev, PRNS)
     launches_per_step = plan.last_launch_count()
 
@@ -277,7 +336,7 @@ def main():
     for _ in range(args.steps):
         flush_l2()
         t0 = time.perf_counter()
-        A.acquire_b(plan, host.numpy(), PRNS)
+        A.acquire_b(plan, host_np, PRNS)
         e2e_s.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e_s)
     if dist is not None:
@@ -297,40 +356,48 @@ def main():
     dom = max(ktimes.items(), key=lambda kv: kv[1][0])
     name, (tot_ms, nl) = dom
     per_launch_s = tot_ms / nl / 1e3
+    per_acq_s = tot_ms / args.steps / 1e3
     n_prn = len(PRNS)
     spc, ndop, F, nb = g.samples_per_code, g.num_doppler_bins, g.fft_size, g.num_blocks
-    # algorithmic bytes per launch of each plain-form kernel (compulsory HBM traffic)
+    spc_eff = g.samples_per_code_eff
+    # algorithmic bytes of each kernel class per acquisition (compulsory HBM traffic of the form):
+    # the coherent tile is written once and read once per step, the accumulator written once
     alg_bytes = {
-        "tile": n_prn * ndop * spc * 8 + ndop * F * 8 + n_prn * nb * F * 8,        # T write + S, C* reads
-        "column": n_prn * ndop * spc * 8 + n_prn * ndop * spc * 4 * 2,              # T read + acc read/write
-        "frontend": n_nc * N_COH * spc * 4 + n_nc * ndop * F * 8,
-        "stats": n_prn * ndop * spc * 4,
+        "tile": n_nc * (n_prn * ndop * spc * 8 + ndop * F * 8) + n_prn * nb * F * 8,
+        "column": n_nc * n_prn * ndop * spc * 8 + n_prn * ndop * spc_eff * 4,
+        "frontend": n_nc * N_COH * spc * ci16.itemsize * 2 + n_nc * ndop * F * 8,
+        "stats": n_prn * ndop * spc_eff * 4,
         # fused: input spectra + code spectra reads, one accumulator write (the algorithmic minimum)
-        "fused": n_nc * ndop * F * 8 + n_prn * nb * F * 8 + n_prn * ndop * spc * 4,
+        "fused": n_nc * ndop * F * 8 + n_prn * nb * F * 8 + n_prn * ndop * spc_eff * 4,
     }
-    # FP32 FFT work per launch (5 N log2 N per complex FFT + 6 per complex multiply)
+    # FP32 work per acquisition (5 N log2 N per complex FFT + 6 per complex multiply + 3 per |x|^2;
+    # the sign / rotation stages run one ndop-point FFT per candidate pattern and bit edge)
     fft_flops = lambda n: 5.0 * n * math.log2(n)
+    n_cand = (g.num_secondary_rotations * (1 << (g.num_data_bits - 1)) * g.bit_edge_search_steps
+              if g.path != 0 else 1)
     flops = {
-        "tile": n_prn * ndop * nb * (fft_flops(F) + 6 * F),
-        "column": n_prn * spc * (fft_flops(ndop) + 3 * ndop),
-        "fused": n_nc * n_prn * (ndop * nb * (fft_flops(F) + 6 * F) + spc * (fft_flops(ndop) + 3 * ndop)),
+        "tile": n_nc * n_prn * ndop * nb * (fft_flops(F) + 6 * F),
+        "column": n_nc * n_prn * spc * n_cand * (fft_flops(ndop) + 3 * ndop),
     }
+    flops["fused"] = flops["tile"] + flops["column"]
     ab = alg_bytes.get(name)
-    achieved = ab / per_launch_s / 1e9 if ab else None
+    achieved = ab / per_acq_s / 1e9 if ab else None
     roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
-            "per_launch_ms": per_launch_s * 1e3, "algorithmic_bytes_per_launch": ab,
-            "fp32_tflops": (flops[name] / per_launch_s / 1e12) if name in flops else None,
+            "per_launch_ms": per_launch_s * 1e3, "launches_per_step": nl / args.steps,
+            "algorithmic_bytes_per_step": ab,
+            "fp32_tflops": (flops[name] / per_acq_s / 1e12) if name in flops else None,
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()}}
 
     cpu = None
     if not args.no_cpu_baseline:
         ts = cpu_port_time_per_prn(ci16, 1)
-        per_acq = ts[0] * n_prn
+        n_s, scale = cpu_port_sample()
+        per_acq = ts[0] * scale
         cpu = {"value": 1.0 / per_acq, "unit": "acq/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "oracle FP32 numpy/scipy restatement, 1 PRN x 8 accumulation steps, x32 PRNs "
-                         "(scipy.fft workers=-1)"}
+               "sample": f"oracle FP32 numpy/scipy restatement, 1 PRN x {n_s} accumulation step(s), scaled to 32 PRNs "
+                         "x all steps (scipy.fft workers=-1)"}
     samples = n_nc * N_COH * spc
     det = [r.prn for r in res if A.is_detected(r)]
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s", "n_gpus": world,
