@@ -97,6 +97,18 @@ def as_complex64(sig):
     return (sig[:, 0].astype(np.float32) + 1j * sig[:, 1].astype(np.float32)).astype(np.complex64)
 
 
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per accumulation step measured by ncu for (kernel, workload), or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        f = line.split()
+        if len(f) == 3 and not line.startswith("#") and f[0] == kernel and f[1] == workload:
+            return int(f[2])
+    return None
+
+
 def peaks():
     p = {}
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -382,8 +394,11 @@ def main():
     flops["fused"] = flops["tile"] + flops["column"]
     ab = alg_bytes.get(name)
     achieved = ab / per_acq_s / 1e9 if ab else None
+    tps = ncu_traffic(name, WORKLOAD)
     roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-            "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+            "frac": (achieved / hbm_peak) if achieved else None,
+            "traffic": (tps * n_nc / (nl / args.steps)) if tps else None,
+            "traffic_source": "ncu capture of a 2-step case scaled to the launch's steps" if tps else None,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
             "per_launch_ms": per_launch_s * 1e3, "launches_per_step": nl / args.steps,
             "algorithmic_bytes_per_step": ab,
