@@ -62,7 +62,9 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_plan_doppler_freqs", "acq_acquire", "acq_acquire_device_async", "acq_fetch_results",
             "acq_plan_stream", "acq_plan_last_launch_count", "acq_cfar_threshold", "acq_gen_code",
             "acq_last_error", "acq_version", "acq_plan_set_kernel_timing", "acq_plan_kernel_times",
-            "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc", "acq_plan_set_option"]
+            "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc", "acq_plan_set_option",
+            "acq_batch_create", "acq_batch_destroy", "acq_batch_input_ptr", "acq_batch_upload", "acq_batch_launch",
+            "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count"]
 ACQ_OPT_FORM = 0
 ACQ_FORM_FUSED, ACQ_FORM_PLAIN = 0, 1
 KERNEL_KINDS = 8

@@ -89,3 +89,44 @@ def random_sats(rng: np.random.Generator, prns, cn0_range, doppler_max, code_len
                              float(rng.uniform(0, code_length)), float(rng.uniform(0, 2 * math.pi)), True,
                              float(rng.uniform(0, bit_period_s)) if bit_period_s > 0 else 0.0))
     return out
+
+
+def ragged_batch(seed: int = 3, n_recordings: int = 64, n_antennas: int = 4, max_nnc: int = 8):
+    """Seeded ragged batch: recordings of uneven length (2-80 ms) from several antennas mixing
+    GPS L1 C/A (5 MHz), Galileo E1B (12 MHz, synthetic codes) and GPS L5I (25 MHz, NH10).
+
+    Returns a list of dicts: system, fs, samples (complex64), prns, n_coh, n_nc, cov, sats, antenna.
+    8-32 PRNs per recording, 0-6 present at C/N0 30-48 dB-Hz, Doppler +-8 kHz. Coherent periods:
+    1 for L1 C/A and E1B; 10 for L5I recordings of >= 20 ms (secondary-code search), else 1.
+    Accumulations: floor(length / coherent time), capped at ``max_nnc``.
+    """
+    from .api import GalileoE1B, GPSL1CA, GPSL5I
+    rng = np.random.default_rng(seed)
+    kinds = [("GPSL1CA", GPSL1CA(), 5e6, 32), ("GalileoE1B", GalileoE1B(), 12e6, 36), ("GPSL5I", GPSL5I(), 25e6, 32)]
+    # one satellite geometry per (antenna, system): same PRNs/Dopplers, per-antenna phases
+    geo = {}
+    for a in range(n_antennas):
+        for name, sysm, _, maxprn in kinds:
+            npres = int(rng.integers(0, 7))
+            present = rng.choice(np.arange(1, maxprn + 1), size=npres, replace=False).tolist()
+            geo[(a, name)] = [(int(p), float(rng.uniform(30, 48)), float(rng.uniform(-8000, 8000)),
+                               float(rng.uniform(0, sysm.code_length))) for p in present]
+    out = []
+    for i in range(n_recordings):
+        name, sysm, fs, maxprn = kinds[i % 3]
+        ant = (i // 3) % n_antennas
+        length_ms = float(rng.uniform(2.0, 80.0))
+        t_code_ms = 1000.0 * sysm.code_length / sysm.code_frequency
+        n_coh = 10 if (name == "GPSL5I" and length_ms >= 20.0) else 1
+        t_coh = n_coh * t_code_ms
+        n_nc = int(max(1, min(max_nnc, math.floor(length_ms / t_coh))))
+        spc = int(math.ceil(sysm.code_length / sysm.code_frequency * fs))
+        n = max(int(length_ms * 1e-3 * fs), n_nc * n_coh * spc)
+        sats = [Satellite(p, c, d, cp, float(rng.uniform(0, 2 * math.pi)), True, 0.0) for (p, c, d, cp) in geo[(ant, name)]]
+        x = synth(sysm, fs, n, sats, seed * 1000 + i).astype(np.complex64)
+        n_prn = int(rng.integers(8, 33))
+        searched = set(rng.choice(np.arange(1, maxprn + 1), size=min(n_prn, maxprn), replace=False).tolist())
+        searched |= {s.prn for s in sats}
+        out.append(dict(system=sysm, fs=fs, samples=x, prns=sorted(int(p) for p in searched), n_coh=n_coh,
+                        n_nc=n_nc, cov=8000.0, sats=sats, antenna=ant, length_ms=length_ms))
+    return out

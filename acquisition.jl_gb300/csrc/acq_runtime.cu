@@ -288,7 +288,9 @@ void setup_col_tma(acq_plan* P, int n_prns) {
     ColTmaFn fn = pick_col_tma(g.ndop);
     if (!fn || (g.spc % 2) != 0) return;
     const size_t tall = sizeof(float2) * (size_t)g.n_nc * n_prns * g.ndop * g.spc;
-    if (tall > (24ull << 30)) return;
+    size_t cap = 4ull << 30;   // all-steps tile buffer per plan (batches hold many plans)
+    if (const char* e = std::getenv("ACQ_TALL_CAP_GB")) cap = static_cast<size_t>(std::atof(e) * (1ull << 30));
+    if (tall > cap) return;
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return;
     int H = 0;
@@ -472,12 +474,26 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     CK(cudaStreamSynchronize(P->stream));
 }
 
-void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples, const int32_t* prns, int n,
-                     double interm_freq, uint32_t flags) {
+// Device-resident arguments of one acquisition's launch sequence.
+struct LaunchArgs {
+    int n = 0;
+    const int* d_slots = nullptr;
+    const int* d_prn_ids = nullptr;
+    const float* d_if_off = nullptr;
+    int use_if = 0;
+    float if_step = 0.f;
+    double interm_freq = 0.0;
+    uint32_t flags = 0;
+    acq_result* d_res = nullptr;
+};
+
+// Validation and host-side constants of acquire! (src/acquire.jl:62-72, :96-97).
+void prepare_request(const acq_plan* P, int64_t n_samples, const int32_t* prns, int n, double interm_freq,
+                     std::vector<int>& slots, std::vector<float>& offs, int& use_if, float& if_step) {
     const Geometry& g = P->g;
     const int64_t seg_len = static_cast<int64_t>(g.n_coh) * g.spc;
-    // src/acquire.jl:62-72
-    std::vector<int> slots(n);
+    if (n <= 0) throw AcqError(ACQ_ERR_ARGUMENT, "no PRNs requested");
+    slots.assign(n, 0);
     for (int i = 0; i < n; ++i) {
         auto it = std::find(P->prns.begin(), P->prns.end(), prns[i]);
         if (it == P->prns.end()) {
@@ -495,16 +511,9 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
                                                  std::to_string(nseg) + " full segments of " + std::to_string(seg_len) +
                                                  ", but plan.num_noncoherent_accumulations=" + std::to_string(g.n_nc) +
                                                  ". Provide a longer signal.");
-    if (n <= 0) throw AcqError(ACQ_ERR_ARGUMENT, "no PRNs requested");
-    CK(cudaSetDevice(P->device));
-    cudaStream_t st = P->stream;
-    int64_t L = 0;
-    CK(cudaMemcpyAsync(P->slots.p, slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(P->prn_ids.p, prns, sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    // IF wipe-off constants in FP32, src/acquire.jl:96-97
-    const int use_if = interm_freq != 0.0;
-    float if_step = 0.f;
-    std::vector<float> offs(g.n_nc, 0.f);
+    use_if = interm_freq != 0.0;
+    if_step = 0.f;
+    offs.assign(g.n_nc, 0.f);
     if (use_if) {
         if_step = static_cast<float>(-2.0 * M_PI * interm_freq / P->desc.sampling_freq_hz);
         for (int m = 0; m < g.n_nc; ++m) {
@@ -512,12 +521,23 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
             volatile float prod = seg0 * if_step;
             offs[m] = prod;
         }
-        CK(cudaMemcpyAsync(P->if_off.p, offs.data(), sizeof(float) * g.n_nc, cudaMemcpyHostToDevice, st));
     }
+}
+
+// The whole launch sequence of one acquisition on `st` (capturable into a CUDA graph: no host
+// memory is touched). Returns the number of this library's kernel launches.
+int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtype, const LaunchArgs& a) {
+    const Geometry& g = P->g;
+    const int64_t seg_len = static_cast<int64_t>(g.n_coh) * g.spc;
+    const int n = a.n;
+    const uint32_t flags = a.flags;
+    const int use_if = a.use_if;
+    const float if_step = a.if_step;
+    int64_t L = 0;
     const int G = g.n_coh * g.nb;
     t_begin(P, ACQ_KERNEL_FRONTEND);
     k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF, P->S.as<float2>(),
-                                                            use_if, if_step, P->if_off.as<float>());
+                                                            use_if, if_step, a.d_if_off);
     t_end(P);
     ++L;
     const float inv_F = 1.0f / static_cast<float>(g.fft_size);
@@ -528,7 +548,7 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
         FusedParams fp{};
         fp.G = G; fp.nb = g.nb; fp.bs = g.bs; fp.spc = g.spc; fp.spc_eff = g.spc_eff; fp.n_nc = g.n_nc;
         fp.rpc = P->fusedRPC; fp.cpc = P->fusedCPC; fp.nf = P->fusedNF; fp.halo = P->fusedH; fp.inv_F = inv_F;
-        fp.S = P->S.as<float2>(); fp.C = P->conj.as<float2>(); fp.slots = P->slots.as<int>();
+        fp.S = P->S.as<float2>(); fp.C = P->conj.as<float2>(); fp.slots = a.d_slots;
         fp.twF = P->fftF.tw; fp.twD = P->fftD.tw; fp.drift = P->drift.as<int>(); fp.acc = P->accb.as<float>();
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g.nb * P->fusedCL, n, 1);
@@ -553,7 +573,7 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
         const int nprn = static_cast<int>(P->prns.size());
         t_begin(P, ACQ_KERNEL_TILE);
         P->tile_fs<<<dim3(G, n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
-            P->S.as<float2>(), P->conj.as<float2>(), P->slots.as<int>(), G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF,
+            P->S.as<float2>(), P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF,
             inv_F, P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
         t_end(P);
         ++L;
@@ -575,10 +595,10 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
             P->tile_fs<<<dim3(G, n), P->tileThreads, P->smem_tile_fs, st>>>(
-                Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF, inv_F,
+                Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF, inv_F,
                 P->T.as<float2>(), 0, P->tileFS);
         else
-            k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), P->slots.as<int>(), G, g.nb,
+            k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), a.d_slots, G, g.nb,
                                                                g.bs, g.spc, P->fftF, P->tileB, inv_F, P->T.as<float2>());
         t_end(P);
         ++L;
@@ -598,25 +618,25 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
             const int W = P->Wsfs;
             P->sign_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
-                P->edge_step, P->slots.as<int>(), dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+                P->edge_step, a.d_slots, dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 2 && P->rot_fs) {
             const int W = P->Wsfs;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
             P->rot_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), g.n_coh, g.nb, g.bs, g.R, P->combos,
-                g.n_be, P->edge_step, use_max, P->slots.as<int>(), dr, first, P->accb.as<float>(),
+                g.n_be, P->edge_step, use_max, a.d_slots, dr, first, P->accb.as<float>(),
                 P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 1) {
             const int W = P->Wsign;
             k_col_sign<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
-                P->edge_step, P->slots.as<int>(), dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+                P->edge_step, a.d_slots, dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
         } else {
             const int W = P->Wsign;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
             k_col_rot<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, P->pats.as<float>(), g.n_coh, g.nb, g.bs, g.R, P->combos,
-                g.n_be, P->edge_step, use_max, P->slots.as<int>(), dr, first, P->accb.as<float>(),
+                g.n_be, P->edge_step, use_max, a.d_slots, dr, first, P->accb.as<float>(),
                 P->winb.as<uint16_t>(), g.spc_eff);
         }
         t_end(P);
@@ -642,26 +662,183 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
     EP.doppler_first = g.doppler_first; EP.doppler_step = g.doppler_step; EP.cfar_thr = g.cfar_thr;
     t_begin(P, ACQ_KERNEL_EXTRACT);
     k_extract<<<n, kThreads, 0, st>>>(P->accb.as<float>(), P->winb.as<uint16_t>(), P->rowpart.as<double>(),
-                                      P->colsum.as<double>(), P->peakpart.as<unsigned long long>(), P->prn_ids.as<int>(),
-                                      EP, P->res.as<acq_result>());
+                                      P->colsum.as<double>(), P->peakpart.as<unsigned long long>(), a.d_prn_ids,
+                                      EP, a.d_res);
     t_end(P);
     ++L;
     if (g.R > 1) {
         t_begin(P, ACQ_KERNEL_SECONDARY);
         k_secondary_prompt<<<dim3(n, g.R), kThreads, 0, st>>>(d_in, dtype, P->chips.as<int8_t>(), P->chips_len,
-                                                              P->slots.as<int>(), g.spc, P->desc.sampling_freq_hz,
-                                                              P->sys->code_freq, interm_freq, P->res.as<acq_result>(),
+                                                              a.d_slots, g.spc, P->desc.sampling_freq_hz,
+                                                              P->sys->code_freq, a.interm_freq, a.d_res,
                                                               P->zs.as<double2>(), g.R);
         k_secondary_argmax<<<(n + 127) / 128, 128, 0, st>>>(P->zs.as<double2>(), P->sec.as<int8_t>(), g.R,
-                                                            P->res.as<acq_result>(), n);
+                                                            a.d_res, n);
         t_end(P);
         L += 2;
     }
     CK(cudaGetLastError());
-    P->launches = L;
+    return L;
+}
+
+void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples, const int32_t* prns, int n,
+                     double interm_freq, uint32_t flags) {
+    std::vector<int> slots;
+    std::vector<float> offs;
+    LaunchArgs a;
+    prepare_request(P, n_samples, prns, n, interm_freq, slots, offs, a.use_if, a.if_step);
+    CK(cudaSetDevice(P->device));
+    cudaStream_t st = P->stream;
+    CK(cudaMemcpyAsync(P->slots.p, slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(P->prn_ids.p, prns, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    if (a.use_if) CK(cudaMemcpyAsync(P->if_off.p, offs.data(), sizeof(float) * offs.size(), cudaMemcpyHostToDevice, st));
+    a.n = n;
+    a.d_slots = P->slots.as<int>();
+    a.d_prn_ids = P->prn_ids.as<int>();
+    a.d_if_off = P->if_off.as<float>();
+    a.interm_freq = interm_freq;
+    a.flags = flags;
+    a.d_res = P->res.as<acq_result>();
+    P->launches = launch_sequence(P, st, d_in, dtype, a);
     P->last_n = n;
     P->last_flags = flags;
     P->req_prns.assign(prns, prns + n);
+}
+
+}  // namespace
+
+struct acq_batch {
+    int device = 0;
+    cudaStream_t s0 = nullptr;
+    std::vector<cudaStream_t> branch;
+    std::vector<cudaEvent_t> events;
+    struct Item {
+        acq_plan* plan;
+        int dtype;
+        int64_t n_samples;
+        size_t in_off, in_bytes;
+        int n, res_off, branch;
+        LaunchArgs args;
+        size_t meta_slots, meta_ids, meta_if;
+    };
+    std::vector<Item> items;
+    DevBuf arena, meta, res;
+    int total_res = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
+};
+
+namespace {
+
+void batch_build(acq_batch* B, const acq_batch_item* items, int n_items) {
+    if (n_items <= 0) throw AcqError(ACQ_ERR_ARGUMENT, "empty batch");
+    B->device = items[0].plan ? items[0].plan->device : 0;
+    std::vector<acq_plan*> plans;
+    std::vector<unsigned char> hmeta;
+    auto push = [&](const void* p, size_t bytes) {
+        size_t off = (hmeta.size() + 15) & ~size_t(15);
+        hmeta.resize(off + bytes);
+        if (bytes) std::memcpy(hmeta.data() + off, p, bytes);
+        return off;
+    };
+    size_t arena = 0;
+    for (int i = 0; i < n_items; ++i) {
+        const acq_batch_item& it = items[i];
+        if (!it.plan || !it.prns) throw AcqError(ACQ_ERR_ARGUMENT, "batch item " + std::to_string(i) + ": null plan or prns");
+        if (it.plan->device != B->device) throw AcqError(ACQ_ERR_ARGUMENT, "batch plans must share one device");
+        if (it.flags & ACQ_FLAG_STORE_POWER_BINS)
+            throw AcqError(ACQ_ERR_ARGUMENT, "store_power_bins is not available in a batch");
+        acq_batch::Item m{};
+        m.plan = it.plan;
+        m.dtype = it.dtype;
+        m.n_samples = it.n_samples;
+        const Geometry& g = it.plan->g;
+        const int64_t need = static_cast<int64_t>(g.n_nc) * g.n_coh * g.spc;
+        m.in_bytes = sample_bytes(it.dtype) * static_cast<size_t>(std::min<int64_t>(it.n_samples, need));
+        m.in_off = arena;
+        arena += (m.in_bytes + 255) & ~size_t(255);
+        std::vector<int> slots;
+        std::vector<float> offs;
+        prepare_request(it.plan, it.n_samples, it.prns, it.n_prns, it.interm_freq_hz, slots, offs, m.args.use_if,
+                        m.args.if_step);
+        m.n = it.n_prns;
+        m.meta_slots = push(slots.data(), sizeof(int) * slots.size());
+        m.meta_ids = push(it.prns, sizeof(int) * it.n_prns);
+        m.meta_if = push(offs.data(), sizeof(float) * offs.size());
+        m.args.n = it.n_prns;
+        m.args.interm_freq = it.interm_freq_hz;
+        m.args.flags = it.flags;
+        m.res_off = B->total_res;
+        B->total_res += it.n_prns;
+        auto pit = std::find(plans.begin(), plans.end(), it.plan);
+        m.branch = static_cast<int>(pit - plans.begin());
+        if (pit == plans.end()) plans.push_back(it.plan);
+        B->items.push_back(m);
+    }
+    CK(cudaSetDevice(B->device));
+    CK(cudaStreamCreateWithFlags(&B->s0, cudaStreamNonBlocking));
+    B->branch.resize(plans.size());
+    for (auto& s : B->branch) CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    B->events.resize(2 * plans.size());
+    for (auto& e : B->events) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    B->arena.ensure(std::max<size_t>(arena, 256));
+    B->meta.ensure(std::max<size_t>(hmeta.size(), 16));
+    CK(cudaMemcpy(B->meta.p, hmeta.data(), hmeta.size(), cudaMemcpyHostToDevice));
+    B->res.ensure(sizeof(acq_result) * B->total_res);
+    unsigned char* mb = B->meta.as<unsigned char>();
+    for (auto& m : B->items) {
+        m.args.d_slots = reinterpret_cast<const int*>(mb + m.meta_slots);
+        m.args.d_prn_ids = reinterpret_cast<const int*>(mb + m.meta_ids);
+        m.args.d_if_off = reinterpret_cast<const float*>(mb + m.meta_if);
+        m.args.d_res = B->res.as<acq_result>() + m.res_off;
+    }
+    // every plan's stream work is finished before the capture reuses its buffers
+    for (acq_plan* P : plans) CK(cudaStreamSynchronize(P->stream));
+    std::vector<bool> timing(plans.size());
+    for (size_t b = 0; b < plans.size(); ++b) {
+        timing[b] = plans[b]->timing;
+        plans[b]->timing = false;
+    }
+    CK(cudaStreamBeginCapture(B->s0, cudaStreamCaptureModeThreadLocal));
+    int64_t L = 0;
+    try {
+        for (size_t b = 0; b < plans.size(); ++b) {
+            CK(cudaEventRecord(B->events[2 * b], B->s0));
+            CK(cudaStreamWaitEvent(B->branch[b], B->events[2 * b], 0));
+        }
+        for (const auto& m : B->items)
+            L += launch_sequence(m.plan, B->branch[m.branch], B->arena.as<unsigned char>() + m.in_off, m.dtype, m.args);
+        for (size_t b = 0; b < plans.size(); ++b) {
+            CK(cudaEventRecord(B->events[2 * b + 1], B->branch[b]));
+            CK(cudaStreamWaitEvent(B->s0, B->events[2 * b + 1], 0));
+        }
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(B->s0, &g);
+        if (g) cudaGraphDestroy(g);
+        for (size_t b = 0; b < plans.size(); ++b) plans[b]->timing = timing[b];
+        throw;
+    }
+    CK(cudaStreamEndCapture(B->s0, &B->graph));
+    for (size_t b = 0; b < plans.size(); ++b) plans[b]->timing = timing[b];
+    CK(cudaGraphInstantiate(&B->exec, B->graph, 0));
+    B->launches = L;
+}
+
+void batch_free(acq_batch* B) {
+    if (!B) return;
+    cudaSetDevice(B->device);
+    if (B->s0) cudaStreamSynchronize(B->s0);
+    if (B->exec) cudaGraphExecDestroy(B->exec);
+    if (B->graph) cudaGraphDestroy(B->graph);
+    for (auto e : B->events) cudaEventDestroy(e);
+    for (auto s : B->branch) cudaStreamDestroy(s);
+    if (B->s0) cudaStreamDestroy(B->s0);
+    B->arena.reset();
+    B->meta.reset();
+    B->res.reset();
+    delete B;
 }
 
 void fetch(acq_plan* P, acq_result* results, float* power_bins) {
@@ -854,6 +1031,94 @@ int acq_plan_last_launch_count(const acq_plan* P, int64_t* count) {
     return guarded([&] {
         if (!P || !count) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         *count = P->launches;
+    });
+}
+
+int acq_batch_create(const acq_batch_item* items, int32_t n_items, acq_batch** out) {
+    return guarded([&] {
+        if (!items || !out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *out = nullptr;
+        acq_batch* B = new acq_batch();
+        try {
+            batch_build(B, items, n_items);
+        } catch (...) {
+            batch_free(B);
+            throw;
+        }
+        *out = B;
+    });
+}
+
+int acq_batch_destroy(acq_batch* B) {
+    batch_free(B);
+    return ACQ_OK;
+}
+
+int acq_batch_input_ptr(acq_batch* B, int32_t item, void** d_ptr) {
+    return guarded([&] {
+        if (!B || !d_ptr || item < 0 || item >= static_cast<int>(B->items.size()))
+            throw AcqError(ACQ_ERR_ARGUMENT, "bad batch item");
+        *d_ptr = B->arena.as<unsigned char>() + B->items[item].in_off;
+    });
+}
+
+int acq_batch_upload(acq_batch* B, const void* const* host) {
+    return guarded([&] {
+        if (!B || !host) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        CK(cudaSetDevice(B->device));
+        for (size_t i = 0; i < B->items.size(); ++i) {
+            if (!host[i]) throw AcqError(ACQ_ERR_ARGUMENT, "null recording for batch item " + std::to_string(i));
+            CK(cudaMemcpyAsync(B->arena.as<unsigned char>() + B->items[i].in_off, host[i], B->items[i].in_bytes,
+                               cudaMemcpyHostToDevice, B->s0));
+        }
+    });
+}
+
+int acq_batch_launch(acq_batch* B) {
+    return guarded([&] {
+        if (!B) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        CK(cudaSetDevice(B->device));
+        CK(cudaGraphLaunch(B->exec, B->s0));
+    });
+}
+
+int acq_batch_fetch(acq_batch* B, acq_result* results) {
+    return guarded([&] {
+        if (!B || !results) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        CK(cudaSetDevice(B->device));
+        CK(cudaMemcpyAsync(results, B->res.p, sizeof(acq_result) * B->total_res, cudaMemcpyDeviceToHost, B->s0));
+        CK(cudaStreamSynchronize(B->s0));
+        for (const auto& m : B->items)
+            if (m.plan->errflag.p) {
+                int e = 0;
+                CK(cudaMemcpy(&e, m.plan->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+                if (e) {
+                    CK(cudaMemset(m.plan->errflag.p, 0, sizeof(int)));
+                    throw AcqError(ACQ_ERR_TIMEOUT, "a bounded wait for a TMA tile gave up");
+                }
+            }
+    });
+}
+
+int acq_batch_run(acq_batch* B, const void* const* host, acq_result* results) {
+    int st = acq_batch_upload(B, host);
+    if (st != ACQ_OK) return st;
+    st = acq_batch_launch(B);
+    if (st != ACQ_OK) return st;
+    return acq_batch_fetch(B, results);
+}
+
+int acq_batch_stream(const acq_batch* B, void** stream) {
+    return guarded([&] {
+        if (!B || !stream) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *stream = static_cast<void*>(B->s0);
+    });
+}
+
+int acq_batch_launch_count(const acq_batch* B, int64_t* count) {
+    return guarded([&] {
+        if (!B || !count) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        *count = B->launches;
     });
 }
 

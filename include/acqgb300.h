@@ -185,6 +185,46 @@ int acq_plan_kernel_times(acq_plan* plan, double* total_ms, int64_t* launches, i
 
 int acq_plan_reset_kernel_times(acq_plan* plan);
 
+/* ---- ragged batches: many recordings, several plans, one CUDA-graph launch ----
+ * Generalises acquire! (src/acquire.jl:54-89) to a list of recordings of uneven length and mixed
+ * systems (one plan per geometry; items may share a plan). The batch packs all inputs into one
+ * device arena, captures every acquisition into a single CUDA graph (one branch per plan; items
+ * that share a plan run in order within their branch) and replays it per batch. The plans must
+ * outlive the batch and be on one device; store_power_bins is not available in a batch. */
+typedef struct acq_batch acq_batch;
+
+typedef struct {
+    acq_plan* plan;
+    int32_t dtype;               /* ACQ_CF32 / ACQ_CI16 / ACQ_CI8 / ACQ_CF64 */
+    int64_t n_samples;           /* length of this recording */
+    const int32_t* prns;         /* requested PRNs (subset of the plan's) */
+    int32_t n_prns;
+    double interm_freq_hz;
+    uint32_t flags;              /* ACQ_FLAG_SUBSAMPLE_INTERP only */
+} acq_batch_item;
+
+int acq_batch_create(const acq_batch_item* items, int32_t n_items, acq_batch** out);
+int acq_batch_destroy(acq_batch* batch);
+
+/* Device address of item i's input slot in the batch arena (for callers that fill it themselves). */
+int acq_batch_input_ptr(acq_batch* batch, int32_t item, void** d_ptr);
+
+/* Copy the items' host recordings into the arena (`host_samples[i]` for item i), asynchronously. */
+int acq_batch_upload(acq_batch* batch, const void* const* host_samples);
+
+/* One graph launch over every item (inputs already in the arena); returns without waiting. */
+int acq_batch_launch(acq_batch* batch);
+
+/* Wait and copy all results (sum of n_prns entries, items in order). */
+int acq_batch_fetch(acq_batch* batch, acq_result* results);
+
+/* upload + launch + fetch. */
+int acq_batch_run(acq_batch* batch, const void* const* host_samples, acq_result* results);
+
+/* The batch's cudaStream_t (opaque) and its kernel launches per graph launch. */
+int acq_batch_stream(const acq_batch* batch, void** stream);
+int acq_batch_launch_count(const acq_batch* batch, int64_t* count);
+
 /* cfar_threshold(pfa, num_cells; num_noncoherent_integrations) — src/cfar.jl:64-85. Host only. */
 int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_integrations, double* out);
 

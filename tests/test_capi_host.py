@@ -28,7 +28,7 @@ def test_library_exports_every_header_symbol():
     lib = C.CDLL(L.LIB_PATH)
     missing = [s for s in sorted(declared) if not hasattr(lib, s)]
     assert not missing, missing
-    assert set(L.EXPORTED) == declared
+    assert set(L.EXPORTED) == declared, set(L.EXPORTED) ^ declared
     assert b"sm_103a" in L.load().acq_version()
 
 
