@@ -24,6 +24,15 @@ using SignFsFn = void (*)(const float2*, int, int, const float2*, const float*, 
 using RotFsFn = void (*)(const float2*, int, int, const float2*, const float*, int, int, int, int, int, int, int, int,
                          const int*, const int*, int, float*, uint16_t*, int);
 
+using RotSbFn = void (*)(const float2*, int, int, const float2*, const float*, int, int, int, int, int, int,
+                         const int*, const int*, int, float*, uint16_t*, int);
+// rotation stage split by (coherent periods, blocks per period); nullptr when not instantiated
+RotSbFn pick_rot_sb(int n_coh, int nb);
+
+using SearchFn = void (*)(SearchParams);
+// warp-per-column search stage (mode 1 sign, 2 rotation); pc = candidates transformed together
+SearchFn pick_search_warp(int mode, int ndop, int* pc);
+
 TileFsFn pick_tile_fs(int fft_size);
 FusedFn pick_fused(int fft_size, int ndop);
 ColFsFn pick_col_fs(int ndop);

@@ -24,6 +24,35 @@ RotFsFn pick_rot_fs(int ndop) {
     }
 }
 
+// PC = 32 / N1 candidates per warp pass fill the lanes of the second FFT pass.
+#define ACQ_SW_CASE(MODE, N)                                                                   \
+    if (ndop == N) {                                                                           \
+        constexpr int n1 = best_split_n1(N), n2 = N / best_split_n1(N);                        \
+        constexpr int pcv = (32 / n1) > 0 ? (32 / n1 > 4 ? 4 : 32 / n1) : 1;                   \
+        *pc = pcv;                                                                             \
+        return &k_col_search_warp<n1, n2, MODE, pcv>;                                          \
+    }
+
+#define ACQ_RSB_CASE(NC, NB) \
+    if (n_coh == NC && nb == NB) return &k_col_rot_sb<NC, NB>;
+
+RotSbFn pick_rot_sb(int n_coh, int nb) {
+    ACQ_RSB_CASE(20, 25) ACQ_RSB_CASE(10, 20) ACQ_RSB_CASE(20, 12) ACQ_RSB_CASE(10, 16) ACQ_RSB_CASE(10, 4)
+    ACQ_RSB_CASE(20, 20) ACQ_RSB_CASE(10, 25) ACQ_RSB_CASE(20, 16) ACQ_RSB_CASE(10, 12) ACQ_RSB_CASE(20, 10)
+    return nullptr;
+}
+
+SearchFn pick_search_warp(int mode, int ndop, int* pc) {
+    if (mode == 2) {
+        ACQ_SW_CASE(2, 40) ACQ_SW_CASE(2, 100) ACQ_SW_CASE(2, 120) ACQ_SW_CASE(2, 160) ACQ_SW_CASE(2, 200)
+        ACQ_SW_CASE(2, 240) ACQ_SW_CASE(2, 250) ACQ_SW_CASE(2, 400) ACQ_SW_CASE(2, 500)
+    } else {
+        ACQ_SW_CASE(1, 40) ACQ_SW_CASE(1, 200) ACQ_SW_CASE(1, 400) ACQ_SW_CASE(1, 500) ACQ_SW_CASE(1, 640)
+        ACQ_SW_CASE(1, 800)
+    }
+    return nullptr;
+}
+
 }  // namespace acq
 
 cudaError_t acq_inst_sign_upload_twiddles(const float2* host, size_t n) {

@@ -620,4 +620,252 @@ __global__ void __launch_bounds__(256) k_col_rot_fs(const float2* __restrict__ T
     }
 }
 
+// ------------------------------------------------------------------ rotation stage, sub-block split
+// Rotation search with the FFT split ndop = NC x NB (NC = coherent periods = sub-blocks, NB =
+// blocks per period): element n2 + NB * p of the column lies in sub-block p, so the pattern
+// sign of sub-block p multiplies pass-1 register p and pass 1 reads the alignment-rotated column
+// straight from the tile (no separate candidate vector). Same result as k_col_rot_fs.
+template <int NC, int NB>
+__global__ void __launch_bounds__(256) k_col_rot_sb(const float2* __restrict__ T, int spc, int W,
+                                                    const float2* __restrict__ twD, const float* __restrict__ pats,
+                                                    int bs, int R, int combos, int n_be, int edge_step, int use_max,
+                                                    const int* __restrict__ slots, const int* __restrict__ drift,
+                                                    int first, float* __restrict__ acc, uint16_t* __restrict__ win,
+                                                    int spc_eff) {
+    constexpr int ND = NC * NB;
+    extern __shared__ float2 sm[];
+    float2* tile = sm;
+    float2* wk = tile + ND * W;
+    float* stage = reinterpret_cast<float*>(wk + ND * W);
+    uint16_t* wst = reinterpret_cast<uint16_t*>(stage + ND * W);
+    int* cro = reinterpret_cast<int*>(wst + ((ND * W + 1) & ~1));
+    float* psm = reinterpret_cast<float*>(cro + W);       // this slot's patterns (n_pat x NC)
+    const int pi = blockIdx.y;
+    const int slot = slots[pi];
+    const int c0 = blockIdx.x * W;
+    const int wv = min(W, spc - c0);
+    const int n_pat = R * combos;
+    const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
+    for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
+        const int e = w / W, t = w - e * W;
+        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < W; t += blockDim.x) {
+        const int pc = c0 + t;
+        const int wrap = ((NB - pc / bs) % NB) * bs + pc % bs;   // src/noncoherent_integration.jl:212-214
+        cro[t] = ((wrap + (bs >> 1)) / bs) % NB;
+    }
+    const float* pp = pats + static_cast<int64_t>(slot) * n_pat * NC;
+    for (int i = threadIdx.x; i < n_pat * NC; i += blockDim.x) psm[i] = pp[i];
+    __syncthreads();
+    float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
+    uint16_t* wp = win + static_cast<int64_t>(pi) * ND * spc_eff;
+    for (int ri = 0; ri < R; ++ri) {
+        for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
+            stage[w] = 0.f;
+            wst[w] = 0;
+        }
+        for (int e = 0; e < n_be; ++e) {
+            for (int d = 0; d < combos; ++d) {
+                const float* pq = psm + (ri * combos + d) * NC;
+                __syncthreads();
+                for (int task = threadIdx.x; task < NB * W; task += blockDim.x) {
+                    const int n2 = task / W, t = task - n2 * W;
+                    int base = (e * edge_step + cro[t]) % ND + n2;
+                    if (base >= ND) base -= ND;
+                    float2 v[NC];
+#pragma unroll
+                    for (int p = 0; p < NC; ++p) {
+                        int row = base + NB * p;
+                        if (row >= ND) row -= ND;
+                        const float sg = pq[p];
+                        const float2 x = tile[row * W + t];
+                        v[p] = make_float2(sg * x.x, sg * x.y);
+                    }
+                    RegFFT<NC, false>::run(v);
+                    static_for<0, NC>([&](auto kc) {
+                        constexpr int k1 = decltype(kc)::value;
+                        constexpr int pr = reg_perm(NC, k1);
+                        float2 y = v[pr];
+                        if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<false>(twD, n2 * k1));
+                        wk[(n2 + NB * k1) * W + t] = y;
+                    });
+                }
+                __syncthreads();
+                for (int task = threadIdx.x; task < NC * W; task += blockDim.x) {
+                    const int k1 = task / W, t = task - k1 * W;
+                    stage_pass2<NC, NB>(wk, W, k1, t, twD, stage, wst, use_max != 0, e * combos + d);
+                }
+            }
+        }
+        __syncthreads();
+        for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
+            const int row = w / W, t = w - row * W;
+            if (t >= wv) continue;
+            int dc = c0 + t + drift[row];
+            if (dc >= spc) dc -= spc;
+            const int64_t idx = static_cast<int64_t>(row) * spc_eff + ri * spc + dc;
+            ap[idx] = first ? stage[w] : ap[idx] + stage[w];
+            wp[idx] = wst[w];
+        }
+    }
+}
+
+// ------------------------------------------------------------------ warp-per-column search stage
+// Sign (MODE 1) or rotation (MODE 2) search with one warp per code-phase column: the CTA loads an
+// (ndop x 8) tile once, then every warp runs all candidates of its column with warp-level sync
+// only, PC candidates at a time (PC two-pass FFTs side by side fill the lanes when ndop is small)
+// and merges them into its private stage in candidate order (strict >, earlier candidate keeps
+// ties), exactly the order of src/noncoherent_integration.jl:60-115 / :183-297 and :654-686.
+// One block barrier per stage slice writes the 8 columns to the accumulator coalesced.
+struct SearchParams {
+    const float2* T;
+    int spc, spc_eff;
+    const float2* twD;
+    const float* pats;       // per slot: n_pat x n_coh
+    int n_pat, n_coh, ndb, n_be, edge_step;
+    int nb, bs, R, combos, use_max;
+    const int* slots;
+    const int* drift;
+    int first;
+    float* acc;
+    uint16_t* win;
+};
+
+template <int N1, int N2, int MODE, int PC>
+__global__ void __launch_bounds__(256) k_col_search_warp(SearchParams sp) {
+    constexpr int ND = N1 * N2;
+    constexpr int TW = 8;                      // columns per CTA = warps per CTA
+    constexpr int half = ND / 2;
+    extern __shared__ float2 sm[];
+    float2* tile = sm;                                       // ND x TW
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float2* wk = tile + ND * TW + wid * (PC * ND);           // PC work vectors of this warp
+    float* pwb = reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) + wid * (PC * ND);
+    float* stage = reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) + TW * PC * ND + wid * ND;
+    uint16_t* wst = reinterpret_cast<uint16_t*>(reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) +
+                                                TW * PC * ND + TW * ND) + wid * ND;
+    const int pi = blockIdx.y;
+    const int slot = sp.slots[pi];
+    const int c0 = blockIdx.x * TW;
+    const int wv = min(TW, sp.spc - c0);
+    const float2* tp = sp.T + static_cast<int64_t>(pi) * ND * sp.spc;
+    for (int w = threadIdx.x; w < ND * TW; w += blockDim.x) {
+        const int e = w / TW, t = w - e * TW;
+        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * sp.spc + c0 + t] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int t = wid;                                        // this warp's column within the tile
+    int cro = 0;
+    if (MODE == 2) {
+        const int pc = c0 + t;
+        const int wrap = ((sp.nb - pc / sp.bs) % sp.nb) * sp.bs + pc % sp.bs;   // src/noncoherent_integration.jl:212-214
+        cro = ((wrap + (sp.bs >> 1)) / sp.bs) % sp.nb;
+    }
+    const float* pp = sp.pats + static_cast<int64_t>(slot) * sp.n_pat * sp.n_coh;
+    const int n_slices = MODE == 2 ? sp.R : 1;
+    const int per_slice = MODE == 2 ? sp.n_be * sp.combos : sp.n_be * sp.n_pat;
+    const int sub_len = ND / sp.ndb;
+    const int coh_per_bit = sp.n_coh / sp.ndb;
+    const bool use_max = MODE == 1 || sp.use_max != 0;
+    float* ap = sp.acc + static_cast<int64_t>(pi) * ND * sp.spc_eff;
+    uint16_t* wp = sp.win + static_cast<int64_t>(pi) * ND * sp.spc_eff;
+    for (int s = 0; s < n_slices; ++s) {
+        if (t < wv) {
+            for (int i = lane; i < ND; i += 32) {
+                stage[i] = 0.f;
+                wst[i] = 0;
+            }
+            for (int cb = 0; cb < per_slice; cb += PC) {
+                const int pc_n = min(PC, per_slice - cb);
+                // ---- build the candidate vectors
+                for (int u = 0; u < pc_n; ++u) {
+                    const int c = cb + u;
+                    float2* x = wk + u * ND;
+                    if (MODE == 2) {
+                        const int e = c / sp.combos, d = c - e * sp.combos;
+                        const float* pq = pp + static_cast<int64_t>(s * sp.combos + d) * sp.n_coh;
+                        const int eff = (e * sp.edge_step + cro) % ND;
+                        for (int i = lane; i < ND; i += 32) {
+                            int row = eff + i;
+                            if (row >= ND) row -= ND;
+                            const float sg = pq[i / sp.nb];
+                            const float2 v = tile[row * TW + t];
+                            x[i] = make_float2(sg * v.x, sg * v.y);
+                        }
+                    } else {
+                        const int e = c / sp.n_pat, p = c - e * sp.n_pat;
+                        const int row_offset = e * sp.edge_step;
+                        for (int i = lane; i < ND; i += 32) {
+                            float2 v = make_float2(0.f, 0.f);
+                            if (i < sub_len) {
+                                for (int b = 0; b < sp.ndb; ++b) {
+                                    const float sg = pp[p * sp.n_coh + b * coh_per_bit];
+                                    const float2 y = tile[((row_offset + b * sub_len + i) % ND) * TW + t];
+                                    v = make_float2(v.x + sg * y.x, v.y + sg * y.y);
+                                }
+                            }
+                            x[i] = v;
+                        }
+                    }
+                }
+                __syncwarp();
+                for (int task = lane; task < pc_n * N2; task += 32) {
+                    const int u = task / N2, n2 = task - u * N2;
+                    fourstep_pass1<N1, N2, false>(wk + u * ND, 1, n2, sp.twD);
+                }
+                __syncwarp();
+                for (int task = lane; task < pc_n * N1; task += 32) {
+                    const int u = task / N1, k1 = task - u * N1;
+                    const float2* x = wk + u * ND;
+                    float2 v[N2];
+#pragma unroll
+                    for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[N2 * k1 + n2];
+                    RegFFT<N2, false>::run(v);
+                    float* pw = pwb + u * ND;
+                    static_for<0, N2>([&](auto kc) {
+                        constexpr int k2 = decltype(kc)::value;
+                        constexpr int pr = reg_perm(N2, k2);
+                        const int om = k1 + N1 * k2;
+                        const float2 xv = v[pr];
+                        pw[om < half ? om + half : om - half] =
+                            __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
+                    });
+                }
+                __syncwarp();
+                // ---- merge in candidate order
+                for (int row = lane; row < ND; row += 32) {
+                    float best = stage[row];
+                    uint16_t bw = wst[row];
+                    for (int u = 0; u < pc_n; ++u) {
+                        const float v = pwb[u * ND + row];
+                        if (!use_max || v > best) {
+                            best = v;
+                            bw = static_cast<uint16_t>(cb + u);
+                        }
+                    }
+                    stage[row] = best;
+                    wst[row] = bw;
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        // ---- coalesced scatter of the TW columns of this slice (drift wraps inside the slice)
+        float* stg0 = reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) + TW * PC * ND;
+        uint16_t* wst0 = reinterpret_cast<uint16_t*>(stg0 + TW * ND);
+        for (int w = threadIdx.x; w < ND * TW; w += blockDim.x) {
+            const int row = w / TW, tc = w - row * TW;
+            if (tc >= wv) continue;
+            int dc = c0 + tc + sp.drift[row];
+            if (dc >= sp.spc) dc -= sp.spc;
+            const int64_t idx = static_cast<int64_t>(row) * sp.spc_eff + s * sp.spc + dc;
+            const float v = stg0[tc * ND + row];
+            ap[idx] = sp.first ? v : ap[idx] + v;
+            wp[idx] = wst0[tc * ND + row];
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace acq

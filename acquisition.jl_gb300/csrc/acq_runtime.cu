@@ -160,6 +160,14 @@ struct acq_plan {
     int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1;
     std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
+    // rotation stage split by sub-blocks
+    RotSbFn rot_sb = nullptr;
+    int Wrsb = 8;
+    size_t smem_rsb = 0;
+    // warp-per-column sign / rotation stage
+    SearchFn search_warp = nullptr;
+    int search_pc = 1;
+    size_t smem_search = 0;
     // specialised sign / rotation stages
     SignFsFn sign_fs = nullptr;
     RotFsFn rot_fs = nullptr;
@@ -386,6 +394,39 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     if (!getenv_flag("ACQ_GENERIC_FFT") && (g.ndop % 2) == 0) {
         if (g.path == 1) P->sign_fs = pick_sign_fs(g.ndop);
         if (g.path == 2) P->rot_fs = pick_rot_fs(g.ndop);
+    }
+    if (g.path == 2 && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT")) {
+        RotSbFn fn = pick_rot_sb(g.n_coh, g.nb);
+        if (fn) {
+            int W = 16;
+            const size_t per = 2 * 8 + 4 + 2;
+            auto need = [&](int w) {
+                return per * (size_t)g.ndop * w + 4 * (size_t)w + 16 +
+                       sizeof(float) * (size_t)g.R * ((size_t)1 << (g.ndb - 1)) * g.n_coh;
+            };
+            while (W > 1 && need(W) > 110 * 1024) W /= 2;
+            if (need(W) <= 200 * 1024) {
+                set_smem((const void*)fn, need(W));
+                P->rot_sb = fn;
+                P->Wrsb = W;
+                P->smem_rsb = need(W);
+            }
+        }
+    }
+    if ((g.path == 1 || g.path == 2) && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT") &&
+        getenv_flag("ACQ_WARP_SEARCH")) {
+        int pc = 1;
+        SearchFn fn = pick_search_warp(g.path, g.ndop, &pc);
+        if (fn) {
+            const size_t smem = sizeof(float2) * (size_t)g.ndop * 8 + 8 * (size_t)pc * g.ndop * (8 + 4) +
+                                8 * (size_t)g.ndop * (4 + 2) + 64;
+            if (smem <= 200 * 1024) {
+                set_smem((const void*)fn, smem);
+                P->search_warp = fn;
+                P->search_pc = pc;
+                P->smem_search = smem;
+            }
+        }
     }
     if (P->sign_fs || P->rot_fs) {
         const size_t per = 2 * 8 + 4 + 2;   // tile + work (float2), stage (float), winner (u16)
@@ -614,6 +655,20 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             const int W = P->Wsimple;
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
+        } else if (g.path == 2 && P->rot_sb && !P->search_warp) {
+            const int W = P->Wrsb;
+            const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            P->rot_sb<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_rsb, st>>>(
+                P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), g.bs, g.R, P->combos, g.n_be,
+                P->edge_step, use_max, a.d_slots, dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+        } else if (g.path != 0 && P->search_warp) {
+            SearchParams sp{};
+            sp.T = P->T.as<float2>(); sp.spc = g.spc; sp.spc_eff = g.spc_eff; sp.twD = P->fftD.tw;
+            sp.pats = P->pats.as<float>(); sp.n_pat = P->n_pat; sp.n_coh = g.n_coh; sp.ndb = g.ndb; sp.n_be = g.n_be;
+            sp.edge_step = P->edge_step; sp.nb = g.nb; sp.bs = g.bs; sp.R = g.R; sp.combos = P->combos;
+            sp.use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0; sp.slots = a.d_slots; sp.drift = dr; sp.first = first;
+            sp.acc = P->accb.as<float>(); sp.win = P->winb.as<uint16_t>();
+            P->search_warp<<<dim3((g.spc + 7) / 8, n), kThreads, P->smem_search, st>>>(sp);
         } else if (g.path == 1 && P->sign_fs) {
             const int W = P->Wsfs;
             P->sign_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
