@@ -24,10 +24,11 @@ using SignFsFn = void (*)(const float2*, int, int, const float2*, const float*, 
 using RotFsFn = void (*)(const float2*, int, int, const float2*, const float*, int, int, int, int, int, int, int, int,
                          const int*, const int*, int, float*, uint16_t*, int);
 
-using RotSbFn = void (*)(const float2*, int, int, const float2*, const float*, int, int, int, int, int, int,
-                         const int*, const int*, int, float*, uint16_t*, int);
-// rotation stage split by (coherent periods, blocks per period); nullptr when not instantiated
-RotSbFn pick_rot_sb(int n_coh, int nb);
+using RotSbFn = void (*)(const float2*, int, const float2*, const float*, int, int, int, int, int, int, const int*,
+                         const int*, int, float*, uint16_t*, int);
+// rotation stage split by (coherent periods, blocks per period); nullptr when not instantiated.
+// *w = columns per block, *threads = block size.
+RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads);
 
 using SearchFn = void (*)(SearchParams);
 // warp-per-column search stage (mode 1 sign, 2 rotation); pc = candidates transformed together

@@ -33,10 +33,16 @@ RotFsFn pick_rot_fs(int ndop) {
         return &k_col_search_warp<n1, n2, MODE, pcv>;                                          \
     }
 
-#define ACQ_RSB_CASE(NC, NB) \
-    if (n_coh == NC && nb == NB) return &k_col_rot_sb<NC, NB>;
+// 16 columns per block up to 384 Doppler bins (wider coalesced accumulator rows), else 8
+#define ACQ_RSB_CASE(NC, NB)                                                \
+    if (n_coh == NC && nb == NB) {                                          \
+        constexpr int kW = (NC * NB <= 384) ? 16 : 8;                       \
+        *w = kW;                                                            \
+        *threads = rot_sb_block(NC, NB, kW);                                \
+        return &k_col_rot_sb<NC, NB, kW>;                                   \
+    }
 
-RotSbFn pick_rot_sb(int n_coh, int nb) {
+RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
     ACQ_RSB_CASE(20, 25) ACQ_RSB_CASE(10, 20) ACQ_RSB_CASE(20, 12) ACQ_RSB_CASE(10, 16) ACQ_RSB_CASE(10, 4)
     ACQ_RSB_CASE(20, 20) ACQ_RSB_CASE(10, 25) ACQ_RSB_CASE(20, 16) ACQ_RSB_CASE(10, 12) ACQ_RSB_CASE(20, 10)
     return nullptr;

@@ -540,8 +540,8 @@ __global__ void __launch_bounds__(256) k_col_sign_fs(const float2* __restrict__ 
         int dc = c0 + t + drift[row];
         if (dc >= spc) dc -= spc;
         const int64_t idx = static_cast<int64_t>(row) * spc_eff + dc;
-        ap[idx] = first ? stage[w] : ap[idx] + stage[w];
-        wp[idx] = wst[w];
+        ap[idx] = (first & 1) ? stage[w] : ap[idx] + stage[w];
+        if (first & 2) wp[idx] = wst[w];
     }
 }
 
@@ -624,54 +624,68 @@ __global__ void __launch_bounds__(256) k_col_rot_fs(const float2* __restrict__ T
 // Rotation search with the FFT split ndop = NC x NB (NC = coherent periods = sub-blocks, NB =
 // blocks per period): element n2 + NB * p of the column lies in sub-block p, so the pattern
 // sign of sub-block p multiplies pass-1 register p and pass 1 reads the alignment-rotated column
-// straight from the tile (no separate candidate vector). Same result as k_col_rot_fs.
-template <int NC, int NB>
-__global__ void __launch_bounds__(256) k_col_rot_sb(const float2* __restrict__ T, int spc, int W,
-                                                    const float2* __restrict__ twD, const float* __restrict__ pats,
-                                                    int bs, int R, int combos, int n_be, int edge_step, int use_max,
-                                                    const int* __restrict__ slots, const int* __restrict__ drift,
-                                                    int first, float* __restrict__ acc, uint16_t* __restrict__ win,
-                                                    int spc_eff) {
+// straight from the tile (no separate candidate vector). Pass-2 thread (k1, t) owns the NB output
+// bins k1 + NC * k2 of column t for every candidate, so the max over data-bit combinations and
+// bit edges (strict '>', earlier candidate wins) stays in registers and is scattered once per
+// rotation. Same result as k_col_rot_fs. `first`: bit 0 = first accumulation step (store instead of
+// add), bit 1 = store the winning candidate (only the last step's survives).
+// Block size for k_col_rot_sb: every pass-2 task (k1, t) needs its own thread; pass 1 loops.
+__host__ __device__ constexpr int rot_sb_block(int nc, int nb, int w) {
+    return nb * w <= 256 ? ((nc > nb ? nc : nb) * w + 31) / 32 * 32 : (nc * w + 31) / 32 * 32;
+}
+
+template <int NC, int NB, int W>
+__global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
+    k_col_rot_sb(const float2* __restrict__ T, int spc, const float2* __restrict__ twD, const float* __restrict__ pats,
+                 int bs, int R, int combos, int n_be, int edge_step, int use_max, const int* __restrict__ slots,
+                 const int* __restrict__ drift, int first, float* __restrict__ acc, uint16_t* __restrict__ win,
+                 int spc_eff) {
     constexpr int ND = NC * NB;
     extern __shared__ float2 sm[];
     float2* tile = sm;
     float2* wk = tile + ND * W;
-    float* stage = reinterpret_cast<float*>(wk + ND * W);
-    uint16_t* wst = reinterpret_cast<uint16_t*>(stage + ND * W);
-    int* cro = reinterpret_cast<int*>(wst + ((ND * W + 1) & ~1));
+    float2* tws = wk + ND * W;                              // ND-point twiddles
+    int* cro = reinterpret_cast<int*>(tws + ND);
     float* psm = reinterpret_cast<float*>(cro + W);       // this slot's patterns (n_pat x NC)
+    const int tid = threadIdx.x;
     const int pi = blockIdx.y;
     const int slot = slots[pi];
     const int c0 = blockIdx.x * W;
     const int wv = min(W, spc - c0);
     const int n_pat = R * combos;
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
-    for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
+    for (int w = tid; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - e * W;
         tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
     }
-    for (int t = threadIdx.x; t < W; t += blockDim.x) {
-        const int pc = c0 + t;
+    for (int i = tid; i < ND; i += blockDim.x) tws[i] = twD[i];
+    if (tid < W) {
+        const int pc = c0 + tid;
         const int wrap = ((NB - pc / bs) % NB) * bs + pc % bs;   // src/noncoherent_integration.jl:212-214
-        cro[t] = ((wrap + (bs >> 1)) / bs) % NB;
+        cro[tid] = ((wrap + (bs >> 1)) / bs) % NB;
     }
     const float* pp = pats + static_cast<int64_t>(slot) * n_pat * NC;
-    for (int i = threadIdx.x; i < n_pat * NC; i += blockDim.x) psm[i] = pp[i];
+    for (int i = tid; i < n_pat * NC; i += blockDim.x) psm[i] = pp[i];
     __syncthreads();
     float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
     uint16_t* wp = win + static_cast<int64_t>(pi) * ND * spc_eff;
+    // pass-2 role (k1, t2) of this thread; pass-1 tasks (n2, t1) loop over the block
+    const int k1 = tid / W, t2 = tid - (tid / W) * W;
+    const bool p2 = tid < NC * W;
     for (int ri = 0; ri < R; ++ri) {
-        for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
-            stage[w] = 0.f;
-            wst[w] = 0;
+        float best[NB];
+        int bwin[NB];
+#pragma unroll
+        for (int k2 = 0; k2 < NB; ++k2) {
+            best[k2] = 0.f;
+            bwin[k2] = 0;
         }
         for (int e = 0; e < n_be; ++e) {
             for (int d = 0; d < combos; ++d) {
                 const float* pq = psm + (ri * combos + d) * NC;
-                __syncthreads();
-                for (int task = threadIdx.x; task < NB * W; task += blockDim.x) {
-                    const int n2 = task / W, t = task - n2 * W;
-                    int base = (e * edge_step + cro[t]) % ND + n2;
+                for (int task = tid; task < NB * W; task += blockDim.x) {
+                    const int n2 = task / W, t1 = task - (task / W) * W;
+                    int base = (e * edge_step + cro[t1]) % ND + n2;
                     if (base >= ND) base -= ND;
                     float2 v[NC];
 #pragma unroll
@@ -679,35 +693,62 @@ __global__ void __launch_bounds__(256) k_col_rot_sb(const float2* __restrict__ T
                         int row = base + NB * p;
                         if (row >= ND) row -= ND;
                         const float sg = pq[p];
-                        const float2 x = tile[row * W + t];
+                        const float2 x = tile[row * W + t1];
                         v[p] = make_float2(sg * x.x, sg * x.y);
                     }
                     RegFFT<NC, false>::run(v);
                     static_for<0, NC>([&](auto kc) {
-                        constexpr int k1 = decltype(kc)::value;
-                        constexpr int pr = reg_perm(NC, k1);
+                        constexpr int kk = decltype(kc)::value;
+                        constexpr int pr = reg_perm(NC, kk);
                         float2 y = v[pr];
-                        if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<false>(twD, n2 * k1));
-                        wk[(n2 + NB * k1) * W + t] = y;
+                        if (kk != 0) y = c_mul(y, tws[n2 * kk]);
+                        wk[(n2 + NB * kk) * W + t1] = y;
                     });
                 }
                 __syncthreads();
-                for (int task = threadIdx.x; task < NC * W; task += blockDim.x) {
-                    const int k1 = task / W, t = task - k1 * W;
-                    stage_pass2<NC, NB>(wk, W, k1, t, twD, stage, wst, use_max != 0, e * combos + d);
+                if (p2) {
+                    const int cand = e * combos + d;
+                    float2 v[NB];
+#pragma unroll
+                    for (int m = 0; m < NB; ++m) v[m] = wk[(NB * k1 + m) * W + t2];
+                    RegFFT<NB, false>::run(v);
+                    static_for<0, NB>([&](auto kc) {
+                        constexpr int k2 = decltype(kc)::value;
+                        constexpr int pr = reg_perm(NB, k2);
+                        const float2 x = v[pr];
+                        const float pw = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+                        const bool take = !use_max || pw > best[k2];
+                        best[k2] = take ? pw : best[k2];
+                        bwin[k2] = take ? cand : bwin[k2];
+                    });
                 }
+                __syncthreads();
+            }
+        }
+        // stage the rotation slice through the (now free) work buffer, then scatter with every thread
+        float* stg = reinterpret_cast<float*>(wk);
+        uint16_t* wst = reinterpret_cast<uint16_t*>(stg + ND * W);
+        if (p2) {
+            constexpr int half = ND / 2;
+#pragma unroll
+            for (int k2 = 0; k2 < NB; ++k2) {
+                const int om = k1 + NC * k2;
+                const int row = om < half ? om + half : om - half;
+                stg[row * W + t2] = best[k2];
+                wst[row * W + t2] = static_cast<uint16_t>(bwin[k2]);
             }
         }
         __syncthreads();
-        for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
-            const int row = w / W, t = w - row * W;
+        for (int w = tid; w < ND * W; w += blockDim.x) {
+            const int row = w / W, t = w - (w / W) * W;
             if (t >= wv) continue;
             int dc = c0 + t + drift[row];
             if (dc >= spc) dc -= spc;
             const int64_t idx = static_cast<int64_t>(row) * spc_eff + ri * spc + dc;
-            ap[idx] = first ? stage[w] : ap[idx] + stage[w];
-            wp[idx] = wst[w];
+            ap[idx] = (first & 1) ? stg[w] : ap[idx] + stg[w];
+            if (first & 2) wp[idx] = wst[w];
         }
+        __syncthreads();
     }
 }
 

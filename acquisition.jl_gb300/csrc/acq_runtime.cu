@@ -162,8 +162,8 @@ struct acq_plan {
     size_t smem_tile_fs = 0, smem_col_fs = 0;
     // rotation stage split by sub-blocks
     RotSbFn rot_sb = nullptr;
-    int Wrsb = 8;
     size_t smem_rsb = 0;
+    int Wrsb = 8, threads_rsb = 256;
     // warp-per-column sign / rotation stage
     SearchFn search_warp = nullptr;
     int search_pc = 1;
@@ -396,21 +396,16 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         if (g.path == 2) P->rot_fs = pick_rot_fs(g.ndop);
     }
     if (g.path == 2 && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT")) {
-        RotSbFn fn = pick_rot_sb(g.n_coh, g.nb);
-        if (fn) {
-            int W = 16;
-            const size_t per = 2 * 8 + 4 + 2;
-            auto need = [&](int w) {
-                return per * (size_t)g.ndop * w + 4 * (size_t)w + 16 +
-                       sizeof(float) * (size_t)g.R * ((size_t)1 << (g.ndb - 1)) * g.n_coh;
-            };
-            while (W > 1 && need(W) > 110 * 1024) W /= 2;
-            if (need(W) <= 200 * 1024) {
-                set_smem((const void*)fn, need(W));
-                P->rot_sb = fn;
-                P->Wrsb = W;
-                P->smem_rsb = need(W);
-            }
+        int w = 8, th = 256;
+        RotSbFn fn = pick_rot_sb(g.n_coh, g.nb, &w, &th);
+        const size_t need = sizeof(float2) * ((size_t)2 * g.ndop * w + g.ndop) + sizeof(int) * w +
+                            sizeof(float) * (size_t)g.R * ((size_t)1 << (g.ndb - 1)) * g.n_coh;
+        if (fn && need <= 200 * 1024) {
+            set_smem((const void*)fn, need);
+            P->rot_sb = fn;
+            P->smem_rsb = need;
+            P->Wrsb = w;
+            P->threads_rsb = th;
         }
     }
     if ((g.path == 1 || g.path == 2) && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT") &&
@@ -645,6 +640,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         ++L;
         const int* dr = P->drift.as<int>() + (size_t)m * g.ndop;
         const int first = m == 0;
+        const bool last = m == g.n_nc - 1;
         t_begin(P, ACQ_KERNEL_COLUMN);
         if (g.path == 0 && P->col_fs) {
             const int W = P->Wfs;
@@ -658,9 +654,10 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         } else if (g.path == 2 && P->rot_sb && !P->search_warp) {
             const int W = P->Wrsb;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
-            P->rot_sb<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_rsb, st>>>(
-                P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), g.bs, g.R, P->combos, g.n_be,
-                P->edge_step, use_max, a.d_slots, dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+            P->rot_sb<<<dim3((g.spc + W - 1) / W, n), P->threads_rsb, P->smem_rsb, st>>>(
+                P->T.as<float2>(), g.spc, P->fftD.tw, P->pats.as<float>(), g.bs, g.R, P->combos, g.n_be,
+                P->edge_step, use_max, a.d_slots, dr, first | (last ? 2 : 0), P->accb.as<float>(),
+                P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path != 0 && P->search_warp) {
             SearchParams sp{};
             sp.T = P->T.as<float2>(); sp.spc = g.spc; sp.spc_eff = g.spc_eff; sp.twD = P->fftD.tw;
@@ -673,7 +670,8 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             const int W = P->Wsfs;
             P->sign_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
-                P->edge_step, a.d_slots, dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
+                P->edge_step, a.d_slots, dr, first | (last ? 2 : 0), P->accb.as<float>(), P->winb.as<uint16_t>(),
+                g.spc_eff);
         } else if (g.path == 2 && P->rot_fs) {
             const int W = P->Wsfs;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
