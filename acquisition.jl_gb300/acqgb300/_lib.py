@@ -58,13 +58,25 @@ class Result(C.Structure):
                 ("detected", C.c_int32), ("reserved", C.c_int32)]
 
 
+class CorrCell(C.Structure):
+    _fields_ = [("prn", C.c_int32), ("reserved", C.c_int32), ("code_phase", C.c_double), ("doppler_hz", C.c_double)]
+
+
+class CorrResult(C.Structure):
+    _fields_ = [("power", C.c_double), ("grad", C.c_double * 2), ("hess", C.c_double * 3), ("z_re", C.c_double),
+                ("z_im", C.c_double), ("iterations", C.c_int32), ("status", C.c_int32)]
+
+
+ACQ_CORR_OK, ACQ_CORR_NOT_CONVERGED, ACQ_CORR_BAD_PRN = 0, 1, 3
+
 EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan_destroy", "acq_plan_get_geometry",
             "acq_plan_doppler_freqs", "acq_acquire", "acq_acquire_device_async", "acq_fetch_results",
             "acq_plan_stream", "acq_plan_last_launch_count", "acq_cfar_threshold", "acq_gen_code",
             "acq_last_error", "acq_version", "acq_plan_set_kernel_timing", "acq_plan_kernel_times",
             "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc", "acq_plan_set_option",
             "acq_batch_create", "acq_batch_destroy", "acq_batch_input_ptr", "acq_batch_upload", "acq_batch_launch",
-            "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count"]
+            "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
+            "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine"]
 ACQ_OPT_FORM = 0
 ACQ_FORM_FUSED, ACQ_FORM_PLAIN = 0, 1
 KERNEL_KINDS = 8
@@ -108,6 +120,13 @@ def load():
     lib.acq_est_signal_noise_power_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_double,
                                                        C.c_int32, C.c_void_p, C.c_void_p]
     lib.acq_plan_set_option.argtypes = [P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
+    lib.acq_corr_create.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int8),
+                                    C.POINTER(P)]
+    lib.acq_corr_destroy.argtypes = [P]
+    lib.acq_corr_eval.argtypes = [P, P, C.c_int32, C.c_int64, C.c_double, P, C.c_int32, C.c_int32, P, P]
+    lib.acq_corr_vjp_samples.argtypes = [P, C.c_int64, C.c_double, P, P, C.c_int32, P, P]
+    lib.acq_corr_refine.argtypes = [P, P, C.c_int32, C.c_int64, C.c_double, P, C.c_int32, C.c_int32, C.c_double,
+                                    C.c_double, C.c_double, C.c_double, P, P]
     lib.acq_version.restype = C.c_char_p
     for name in EXPORTED:
         if name not in ("acq_plan_desc_init", "acq_version"):

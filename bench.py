@@ -57,6 +57,9 @@ CONFIGS = {
     # secondary-code rotation search: GPS L5I 20 MHz, 20 ms x 4, +-10 kHz, CI8 (3-bit)
     "cfg4": dict(workload="gps_l5i_20MHz_20msx4_pm10kHz_32prn_ci8", system="GPSL5I", fs=20e6, n_coh=20, n_nc=4,
                  n_be=1, cov=10000.0, quant="ci8", n_sats=6, cn0=(30.0, 45.0), dmax=10000.0, bit_period=0.01),
+    # differentiable fine search: L1 C/A 10 MHz, 20 ms CF32, 32 PRNs x 1024 (code phase, Doppler) cells
+    "cfg5": dict(workload="gps_l1ca_10MHz_20ms_cf32_32prn_x1024cells_fine", system="GPSL1CA", fs=10e6, n_coh=20,
+                 n_nc=1, n_be=1, cov=7000.0, quant=None, cn0=(40.0, 48.0), dmax=7000.0, cells_per_prn=1024),
 }
 CFG = CONFIGS["cfg2"]
 FS, N_COH, N_NC, COV = CFG["fs"], CFG["n_coh"], CFG["n_nc"], CFG["cov"]
@@ -302,6 +305,175 @@ def run_batch(args, world, rank, local_rank):
     print(json.dumps(line))
 
 
+FINE_FLOPS = {"eval": 34, "hess": 56, "vjp": 19}   # FP32 flops per (cell, sample), see run_fine
+
+
+def fine_input():
+    """cfg5 recording: all 32 PRNs present (C/N0 ~ U[40, 48] dB-Hz, Doppler ~ U[+-7 kHz], code phase
+    ~ U[0, 1023) chips, continuous), data-free 20 ms, unit-power white noise; and 1024 cells per PRN
+    within +-1 code bin (one sample) and +-1 Doppler bin (1/T) of the true parameters."""
+    from acqgb300 import synth
+    import acqgb300 as A
+    rng = np.random.default_rng(SEED)
+    n = int(round(FS * 0.02))
+    sats = [synth.Satellite(p, float(rng.uniform(*CFG["cn0"])), float(rng.uniform(-CFG["dmax"], CFG["dmax"])),
+                            float(rng.uniform(0, 1023)), float(rng.uniform(0, 2 * math.pi)), data_bits=False)
+            for p in PRNS]
+    x = synth.synth(A.GPSL1CA(), FS, n, sats, SEED).astype(np.complex64)
+    m = CFG["cells_per_prn"]
+    chip_bin, dop_bin = 1.023e6 / FS, FS / n
+    prn = np.repeat(PRNS, m)
+    tau = np.concatenate([s.code_phase + rng.uniform(-1, 1, m) * chip_bin for s in sats])
+    dop = np.concatenate([s.doppler + rng.uniform(-1, 1, m) * dop_bin for s in sats])
+    return x, sats, prn, tau, dop
+
+
+def run_fine(args, world, rank, local_rank):
+    """Differentiable fine search (cfg5). A step = for every cell: power and gradient (forward),
+    the adjoint with respect to the 200 000 samples for the loss sum(P) (backward; the code
+    replica is recomputed), and batched Newton refinement from the cell."""
+    import torch
+    import acqgb300 as A
+    from acqgb300 import corr as CR
+    torch.cuda.set_device(local_rank)
+    dev = f"cuda:{local_rank}"
+    x, sats, prn, tau, dop = fine_input()
+    n = x.size
+    corr = CR.Correlator(A.GPSL1CA(), FS, PRNS, device=local_rank)
+    cells = CR.pack_cells(prn, tau, dop)
+    nc = cells.size
+    xd = torch.as_tensor(x, device=dev)
+    cd = corr._cells_dev(cells)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream()
+
+    def step(timing=None):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(st)
+        raw = corr.eval_device(xd, cd, nc, False)
+        ev[1].record(st)
+        r = raw.view(torch.float64)[: nc * 9].view(nc, 9)
+        zbar = (2.0 * torch.complex(r[:, 6], r[:, 7])).to(torch.complex64)
+        corr.vjp_device(n, cd, nc, zbar)
+        ev[2].record(st)
+        c2 = cd.clone()
+        corr.refine_device(xd, c2, nc, max_iterations=20)
+        ev[3].record(st)
+        if timing is not None:
+            timing.append(ev)
+        return c2
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local_rank)
+    evs = []
+    with clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            step(evs)
+        torch.cuda.synchronize()
+    parts = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])] for e in evs])
+    t_step = parts.sum(axis=1).mean() / 1e3
+    t_eval, t_vjp, t_ref = parts.mean(axis=0)
+    hess_ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        corr.eval_device(xd, cd, nc, True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        hess_ms.append(e0.elapsed_time(e1))
+    t_hess = statistics.mean(hess_ms)
+
+    # e2e through the public API: host samples and cells in, host results out, every step
+    xh = torch.from_numpy(x).pin_memory()
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xg = xh.to(dev, non_blocking=True)
+        ev = corr.eval(xg, prn, tau, dop)
+        corr.vjp_samples(n, prn, tau, dop, 2.0 * ev.z).cpu()
+        rf = corr.refine(xg, prn, tau, dop, max_iterations=20)
+        e2e.append(time.perf_counter() - t0)
+    t_e2e = statistics.mean(e2e)
+
+    # quality: Newton from every cell against the maximum reached from the true parameters
+    ml = corr.refine(xd, PRNS, [s.code_phase for s in sats], [s.doppler for s in sats], max_iterations=30)
+    mt = np.repeat(ml.code_phase, CFG["cells_per_prn"])
+    mf = np.repeat(ml.doppler, CFG["cells_per_prn"])
+    same = (np.abs(rf.code_phase - mt) < 2e-3) & (np.abs(rf.doppler - mf) < 0.05)
+    dop_bin = FS / n
+    inner = (np.abs(tau - np.repeat([s.code_phase for s in sats], CFG["cells_per_prn"])) < 0.5 * 1.023e6 / FS) & \
+            (np.abs(dop - np.repeat([s.doppler for s in sats], CFG["cells_per_prn"])) < 0.5 * dop_bin)
+
+    # FP32 results against the FP64 oracle on a sample of cells
+    from oracle import corr_oracle as O
+    from oracle import gnss_codes as G
+    rng = np.random.default_rng(7)
+    pick = rng.choice(nc, 12, replace=False)
+    eh = corr.eval(xd, prn[pick], tau[pick], dop[pick], hessian=True)
+    T = n / FS
+    err = np.zeros(3)
+    for j, i in enumerate(pick):
+        d = O.correlate(x.astype(np.complex128), G.GPSL1CA, int(prn[i]), FS, tau[i], dop[i])
+        P, g, h = O.power_derivatives(d)
+        Ps = ml.power[PRNS.index(int(prn[i]))]
+        err = np.maximum(err, [abs(eh.power[j] - P) / Ps, np.max(np.abs(eh.grad[j] - g) / [Ps, Ps * T]),
+                               np.max(np.abs(eh.hess[j] - h) / [Ps, Ps * T, Ps * T * T])])
+    xb = corr.vjp_samples(n, prn[pick], tau[pick], dop[pick], 2.0 * eh.z).cpu().numpy()
+    xb_ref = O.vjp_samples(n, G.GPSL1CA, FS, [(int(prn[i]), tau[i], dop[i]) for i in pick], 2.0 * eh.z)
+    err_vjp = float(np.max(np.abs(xb - xb_ref)) / np.max(np.abs(xb_ref)))
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        for i in pick[:4]:
+            O.power_derivatives(O.correlate(x, G.GPSL1CA, int(prn[i]), FS, tau[i], dop[i]))
+        t_c = (time.perf_counter() - t0) / 4
+        t0 = time.perf_counter()
+        O.vjp_samples(n, G.GPSL1CA, FS, [(int(prn[i]), tau[i], dop[i]) for i in pick[:4]], np.ones(4))
+        t_v = (time.perf_counter() - t0) / 4
+        t0 = time.perf_counter()
+        its = 0
+        for i in pick[:2]:
+            its += O.newton_refine(x, G.GPSL1CA, int(prn[i]), FS, tau[i], dop[i], max_iter=20)[3]
+        t_r = (time.perf_counter() - t0) / 2
+        cpu = {"value": 1.0 / (t_c + t_v + t_r), "unit": "cells/s", "cores": 1, "kind": "port",
+               "sample": "FP64 numpy oracle: 4 cells of power+gradient+Hessian, 4 cells of the sample adjoint, "
+                         "2 Newton refinements, on 200 000 samples each"}
+    algo = nc * n * (FINE_FLOPS["eval"] + FINE_FLOPS["vjp"])
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    if rank != 0:
+        return
+    ach = nc * n * FINE_FLOPS["hess"] / (t_hess / 1e3) / 1e12
+    line = {"metric": "fine-search cells/s", "value": world * nc / t_step, "unit": "cells/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, CF32, 32 PRNs present)",
+            "config": {"workload": WORKLOAD, "cells": nc, "samples": n,
+                       "step": "forward power+gradient, sample adjoint, Newton refinement (<= 20 iterations)",
+                       "l2": "flushed (256 MB write) before every timed step"},
+            "ms": {"eval": t_eval, "vjp": t_vjp, "refine": t_ref, "eval_with_hessian": t_hess},
+            "gcell_samples_per_s": {"eval": nc * n / (t_eval / 1e3) / 1e9, "eval_with_hessian": nc * n / (t_hess / 1e3) / 1e9,
+                                    "vjp": nc * n / (t_vjp / 1e3) / 1e9},
+            "refine": {"converged": int(np.sum(rf.status == 0)), "mean_iterations": float(rf.iterations.mean()),
+                       "to_peak_all": float(same.mean()), "to_peak_within_half_bin": float(same[inner].mean())},
+            "fp64_error": {"power": err[0], "gradient": err[1], "hessian": err[2], "vjp": err_vjp,
+                           "scale": "power at the peak; per chip, per Hz x T; per chip^2 ... x T^2; max |x_bar|"},
+            "e2e": {"value": world * nc / t_e2e, "unit": "cells/s", "h2d_bytes_per_step": int(x.nbytes + 3 * cells.nbytes + nc * 8),
+                    "d2h_bytes_per_step": int(nc * 72 * 2 + n * 8 + nc * 24), "ms_per_step": t_e2e * 1e3},
+            "gpu_launches": 4 * args.steps,
+            "roofline": {"kernel": "k_corr (power+gradient+Hessian)", "bound": "fp32", "achieved": ach,
+                         "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                         "peak_source": "nominal FP32 CUDA-core rate: 152 SMs x 128 lanes x 2 flops x 2.07 GHz",
+                         "flops_per_cell_sample": FINE_FLOPS, "traffic": None},
+            "cpu_baseline": cpu, "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -329,6 +501,9 @@ def main():
         return
     if args.config == "cfg3":
         run_batch(args, world, rank, local_rank)
+        return
+    if args.config == "cfg5":
+        run_fine(args, world, rank, local_rank)
         return
 
     import torch

@@ -260,6 +260,71 @@ int acq_est_signal_noise_power_noalloc(const float* d_power_bins, int32_t num_do
                                        double sampling_freq_hz, double code_freq_hz, int32_t noise_estimator,
                                        acq_noise_stats* d_out, void* stream);
 
+/* ---- continuous correlator: fine search, gradients, Newton refinement ----
+ *
+ * Extends the grid search with a continuous correlator over (code phase, Doppler):
+ *   phi_n   = code_phase + n * (f_code + doppler * f_code / f_carrier) / fs      [chips]
+ *   theta_n = 2 pi (interm_freq + doppler) n / fs
+ *   z       = sum_n x[n] c(phi_n) exp(-i theta_n),       power P = |z|^2
+ * over the model of src/generate_test_signal.jl:45-68 (the correlation the acquisition grid
+ * samples at integer code bins and Doppler bins). c is the PRN's chip sequence (BOC(1,1) half
+ * chips for Galileo E1B, the secondary code folded in for GPS L5I) smoothed by the quadratic
+ * B-spline centred on each chip, so that P is differentiable twice in code phase and Doppler.
+ * Sums run in FP32 on the device; the derived power, gradient and Hessian are formed in FP64.
+ * Every pointer named d_* is device memory; `stream` is a cudaStream_t (NULL = default
+ * stream). Calls enqueue work and return without waiting. */
+typedef struct acq_corr acq_corr;
+
+typedef struct {
+    int32_t prn;
+    int32_t reserved;       /* 0 */
+    double code_phase;      /* chips at sample 0 */
+    double doppler_hz;      /* carrier Doppler */
+} acq_corr_cell;            /* 24 bytes */
+
+#define ACQ_CORR_OK 0               /* evaluated / converged */
+#define ACQ_CORR_NOT_CONVERGED 1    /* acq_corr_refine ran out of iterations */
+#define ACQ_CORR_BAD_PRN 3          /* the cell's PRN is not in the context: outputs are zero */
+
+typedef struct {
+    double power;           /* P = |z|^2 */
+    double grad[2];         /* dP/d code_phase (per chip), dP/d doppler (per Hz) */
+    double hess[3];         /* d2P/dtau2, d2P/dtau ddoppler, d2P/ddoppler2 (zero unless requested) */
+    double z_re, z_im;      /* correlator output z */
+    int32_t iterations;     /* Newton iterations (acq_corr_refine), 0 for acq_corr_eval */
+    int32_t status;         /* ACQ_CORR_* */
+} acq_corr_result;          /* 72 bytes */
+
+/* A context for `system` at `sampling_freq_hz` over `prns`: uploads the chip tables. `codes`
+ * is NULL (built-in generators) or n_prns x primary-code-length chips of +-1 (as in
+ * acq_plan_create). */
+int acq_corr_create(int32_t system, double sampling_freq_hz, const int32_t* prns, int32_t n_prns,
+                    const int8_t* codes, acq_corr** out);
+int acq_corr_destroy(acq_corr* ctx);
+
+/* Power, gradient (and the Hessian when want_hessian != 0) at every cell.
+ * d_samples: n_samples samples of `dtype` (ACQ_CF32 / ACQ_CI16 / ACQ_CI8 / ACQ_CF64). */
+int acq_corr_eval(acq_corr* ctx, const void* d_samples, int32_t dtype, int64_t n_samples, double interm_freq_hz,
+                  const acq_corr_cell* d_cells, int32_t n_cells, int32_t want_hessian, acq_corr_result* d_out,
+                  void* stream);
+
+/* Adjoint with respect to the samples: d_xbar[n] = sum_cells d_zbar[c] * conj(dz_c / dx[n])
+ * = sum_c zbar_c c(phi_{c,n}) exp(+i theta_{c,n}), written as interleaved float32 re/im
+ * (2 * n_samples floats, overwritten). zbar_c = dL/dRe z_c + i dL/dIm z_c is the cotangent of
+ * z_c (2 * P_bar_c * z_c for a loss on the power). The code replica is recomputed, not read. */
+int acq_corr_vjp_samples(acq_corr* ctx, int64_t n_samples, double interm_freq_hz, const acq_corr_cell* d_cells,
+                         const float* d_zbar, int32_t n_cells, float* d_xbar, void* stream);
+
+/* Batched Newton refinement of the power maximum from every cell (updated in place): Newton
+ * steps on the closed-form gradient and Hessian inside a box trust region of
+ * (max_step_chips, max_step_hz), gradient ascent where the Hessian is not negative definite,
+ * step halving when the power drops; stops when both step components fall below the
+ * tolerances. d_out receives the evaluation at the final point. */
+int acq_corr_refine(acq_corr* ctx, const void* d_samples, int32_t dtype, int64_t n_samples, double interm_freq_hz,
+                    acq_corr_cell* d_cells, int32_t n_cells, int32_t max_iterations, double tol_chips,
+                    double tol_hz, double max_step_chips, double max_step_hz, acq_corr_result* d_out, void* stream);
+
+
 /* Copy the calling thread's last error message (NUL-terminated, truncated to len). */
 int acq_last_error(char* buf, size_t len);
 

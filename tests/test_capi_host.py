@@ -142,3 +142,20 @@ def test_plan_create_fails_loudly_without_gpu():
         pass
     with pytest.raises(A.AcquisitionError):
         A.plan_acquire(A.GPSL1CA(), 4e6, [1])
+
+
+def test_correlator_create_fails_loudly_without_gpu():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    lib = L.load()
+    h = C.c_void_p()
+    prns = (C.c_int32 * 2)(1, 2)
+    st = lib.acq_corr_create(L.ACQ_GPS_L1CA, 10e6, prns, 2, None, C.byref(h))
+    assert st == L.ACQ_ERR_CUDA and h.value is None
+    bad = (C.c_int32 * 1)(40)
+    assert lib.acq_corr_create(L.ACQ_GPS_L1CA, 10e6, bad, 1, None, C.byref(h)) == L.ACQ_ERR_ARGUMENT
+    assert "PRN must be in 1:32" in L.last_error()
