@@ -78,6 +78,8 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
             "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine"]
 ACQ_OPT_FORM = 0
+ACQ_OPT_ROTATION_PRECISION = 1
+ACQ_OPT_MMA_SCALE_LOG2 = 2
 ACQ_FORM_FUSED, ACQ_FORM_PLAIN = 0, 1
 KERNEL_KINDS = 8
 KERNEL_NAMES = ["frontend", "tile", "column", "stats", "extract", "secondary", "fused", "k7"]

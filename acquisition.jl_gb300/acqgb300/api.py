@@ -24,6 +24,9 @@ import numpy as np
 from . import _lib as L
 
 
+PRECISIONS = {"fp32": 0, "fp16": 1, "bf16": 2, "fp16_split": 3, "bf16_split": 4}
+
+
 class ArgumentError(ValueError):
     """Mirror of Julia's ArgumentError (invalid plan or acquire! arguments)."""
 
@@ -236,6 +239,20 @@ class AcquisitionPlan:
         eff = C.c_int64()
         _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_FORM, val, C.byref(eff)))
         return "fused" if eff.value == L.ACQ_FORM_FUSED else "plain"
+
+    def set_rotation_precision(self, precision: str) -> str:
+        """Arithmetic of the secondary-code rotation combine: 'fp32' (FFTs on the CUDA cores, the
+        default) or a tensor-core variant 'fp16', 'bf16', 'fp16_split', 'bf16_split' (sub-block
+        spectra rounded to FP16/BF16, or split hi + lo, FP32 accumulation). Returns the precision
+        in effect ('fp32' where the plan's geometry has no tensor-core variant)."""
+        val = PRECISIONS[precision]
+        eff = C.c_int64()
+        _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_ROTATION_PRECISION, val, C.byref(eff)))
+        return {v: k for k, v in PRECISIONS.items()}[eff.value]
+
+    def set_mma_scale_log2(self, e: int | None):
+        """Power-of-two scale of the spectra before FP16 rounding (None: by input type)."""
+        _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_MMA_SCALE_LOG2, 127 if e is None else int(e), None))
 
     def set_kernel_timing(self, enable: bool = True):
         _check(L.load().acq_plan_set_kernel_timing(self._h, 1 if enable else 0))

@@ -46,7 +46,7 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
     dev_obj = os.path.join(BUILD_DIR, "acq_runtime.o")
     na_obj = os.path.join(BUILD_DIR, "acq_noalloc.o")
     corr_obj = os.path.join(BUILD_DIR, "acq_corr.o")
-    inst = ["acq_inst_tile", "acq_inst_col", "acq_inst_sign"]
+    inst = ["acq_inst_tile", "acq_inst_col", "acq_inst_sign", "acq_inst_mma"]
     inst_objs = [os.path.join(BUILD_DIR, f"{n}.o") for n in inst]
     host_cmd = ["g++", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", *opt,
                 f"-I{INCLUDE}", "-c", os.path.join(CSRC, "acq_host.cpp"), "-o", host_obj]

@@ -30,6 +30,12 @@ using RotSbFn = void (*)(const float2*, int, const float2*, const float*, int, i
 // *w = columns per block, *threads = block size.
 RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads);
 
+struct RotMmaParams;
+using RotMmaFn = void (*)(RotMmaParams);
+// tensor-core rotation combine for (coherent periods, blocks per period, candidates) at an
+// ACQ_PREC_* precision other than FP32; nullptr when not instantiated; *smem = dynamic bytes.
+RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int prec, size_t* smem);
+
 using SearchFn = void (*)(SearchParams);
 // warp-per-column search stage (mode 1 sign, 2 rotation); pc = candidates transformed together
 SearchFn pick_search_warp(int mode, int ndop, int* pc);
@@ -46,3 +52,4 @@ RotFsFn pick_rot_fs(int ndop);
 cudaError_t acq_inst_tile_upload_twiddles(const float2* host, size_t n);
 cudaError_t acq_inst_col_upload_twiddles(const float2* host, size_t n);
 cudaError_t acq_inst_sign_upload_twiddles(const float2* host, size_t n);
+cudaError_t acq_inst_mma_upload_twiddles(const float2* host, size_t n);

@@ -1,0 +1,36 @@
+// acq_inst_mma.cu — tensor-core rotation combine (k_rot_mma) for the instantiated geometries.
+#include "acqgb300.h"
+#include "acq_inst.h"
+#include "acq_mma.cuh"
+
+namespace acq {
+
+namespace {
+template <int NC, int NB, int QP>
+RotMmaFn pick_prec(int prec, size_t* smem) {
+    using S = RotMmaShape<NC, NB, QP>;
+    switch (prec) {
+        case ACQ_PREC_FP16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, 0, 1>;
+        case ACQ_PREC_BF16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, 1, 1>;
+        case ACQ_PREC_FP16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, 0, 2>;
+        case ACQ_PREC_BF16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, 1, 2>;
+        default: return nullptr;
+    }
+}
+}  // namespace
+
+#define ACQ_MMA_CASE(NC, NB, QP) \
+    if (n_coh == NC && nb == NB && qp == QP) return pick_prec<NC, NB, QP>(prec, smem);
+
+RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int prec, size_t* smem) {
+    const int qp = (n_candidates + 7) / 8 * 8;
+    ACQ_MMA_CASE(20, 25, 24) ACQ_MMA_CASE(10, 20, 16) ACQ_MMA_CASE(20, 12, 24) ACQ_MMA_CASE(10, 16, 16)
+    ACQ_MMA_CASE(10, 4, 16) ACQ_MMA_CASE(20, 20, 24)
+    return nullptr;
+}
+
+}  // namespace acq
+
+cudaError_t acq_inst_mma_upload_twiddles(const float2* host, size_t n) {
+    return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
+}

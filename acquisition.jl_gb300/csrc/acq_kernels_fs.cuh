@@ -451,6 +451,48 @@ __global__ void __launch_bounds__(256) k_fused_simple(FusedParams fp) {
 // candidate (bit edge, data-bit pattern or secondary-code rotation) the zero-padded / pattern-
 // weighted column is transformed in place with the two-pass register FFT and max-reduced (or
 // stored) into the stage in sorted-Doppler order, exactly as k_col_sign / k_col_rot.
+// Scatter of a staged (rows x W) slice into the accumulator at column offset col0 with the
+// destination-row drift: dc = (c0 + t + drift[row]) mod spc. Read-modify-writes are issued in
+// batches of 8 (all loads, then all stores) so that their latencies overlap. `first`: bit 0 =
+// store instead of add, bit 1 = also store the winning candidate.
+__device__ __forceinline__ void scatter_rmw_rt(const float* __restrict__ stg, const uint16_t* __restrict__ wst,
+                                               int n, int W, int tid, int nthr, int wv, int c0, int spc,
+                                               int64_t spc_eff, int64_t col0, const int* __restrict__ drift,
+                                               int first, float* __restrict__ ap, uint16_t* __restrict__ wp) {
+    for (int w0 = tid; w0 < n; w0 += 8 * nthr) {
+        int64_t idx[8];
+        bool ok[8];
+        float old[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int w = w0 + u * nthr;
+            const int row = w / W, t = w - (w / W) * W;
+            ok[u] = w < n && t < wv;
+            int dc = c0 + t + (ok[u] ? drift[row] : 0);
+            dc = dc >= spc ? dc - spc : dc;
+            idx[u] = static_cast<int64_t>(row) * spc_eff + col0 + dc;
+        }
+        if (!(first & 1)) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) old[u] = ok[u] ? ap[idx[u]] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (!ok[u]) continue;
+            const int w = w0 + u * nthr;
+            ap[idx[u]] = (first & 1) ? stg[w] : old[u] + stg[w];
+            if (first & 2) wp[idx[u]] = wst[w];
+        }
+    }
+}
+template <int W>
+__device__ __forceinline__ void scatter_rmw(const float* __restrict__ stg, const uint16_t* __restrict__ wst, int n,
+                                            int tid, int nthr, int wv, int c0, int spc, int64_t spc_eff,
+                                            int64_t col0, const int* __restrict__ drift, int first,
+                                            float* __restrict__ ap, uint16_t* __restrict__ wp) {
+    scatter_rmw_rt(stg, wst, n, W, tid, nthr, wv, c0, spc, spc_eff, col0, drift, first, ap, wp);
+}
+
 template <int N1, int N2>
 __device__ __forceinline__ void stage_pass2(float2* wk, int W, int k1, int t, const float2* __restrict__ twD,
                                             float* stage, uint16_t* wst, bool use_max, int cand) {
@@ -534,15 +576,7 @@ __global__ void __launch_bounds__(256) k_col_sign_fs(const float2* __restrict__ 
     }
     float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
     uint16_t* wp = win + static_cast<int64_t>(pi) * ND * spc_eff;
-    for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
-        const int row = w / W, t = w - row * W;
-        if (t >= wv) continue;
-        int dc = c0 + t + drift[row];
-        if (dc >= spc) dc -= spc;
-        const int64_t idx = static_cast<int64_t>(row) * spc_eff + dc;
-        ap[idx] = (first & 1) ? stage[w] : ap[idx] + stage[w];
-        if (first & 2) wp[idx] = wst[w];
-    }
+    scatter_rmw_rt(stage, wst, ND * W, W, threadIdx.x, blockDim.x, wv, c0, spc, spc_eff, 0, drift, first, ap, wp);
 }
 
 template <int N1, int N2>
@@ -739,15 +773,7 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
             }
         }
         __syncthreads();
-        for (int w = tid; w < ND * W; w += blockDim.x) {
-            const int row = w / W, t = w - (w / W) * W;
-            if (t >= wv) continue;
-            int dc = c0 + t + drift[row];
-            if (dc >= spc) dc -= spc;
-            const int64_t idx = static_cast<int64_t>(row) * spc_eff + ri * spc + dc;
-            ap[idx] = (first & 1) ? stg[w] : ap[idx] + stg[w];
-            if (first & 2) wp[idx] = wst[w];
-        }
+        scatter_rmw<W>(stg, wst, ND * W, tid, blockDim.x, wv, c0, spc, spc_eff, ri * spc, drift, first, ap, wp);
         __syncthreads();
     }
 }

@@ -16,6 +16,7 @@
 
 #include "acq_host.h"
 #include "acq_inst.h"
+#include "acq_mma.cuh"
 #include "acq_kernels.cuh"
 
 using namespace acq;
@@ -94,7 +95,8 @@ void upload_reg_twiddles() {
             double a = -2.0 * M_PI * static_cast<double>(e) / static_cast<double>(n);
             h[reg_tw_offset(n) + e] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
         }
-    for (auto up : {acq_inst_tile_upload_twiddles, acq_inst_col_upload_twiddles, acq_inst_sign_upload_twiddles}) {
+    for (auto up : {acq_inst_tile_upload_twiddles, acq_inst_col_upload_twiddles, acq_inst_sign_upload_twiddles,
+                    acq_inst_mma_upload_twiddles}) {
         cudaError_t e = up(h.data(), h.size());
         if (e != cudaSuccess) throw CudaError(std::string("twiddle upload: ") + cudaGetErrorString(e));
     }
@@ -163,6 +165,11 @@ struct acq_plan {
     // rotation stage split by sub-blocks
     RotSbFn rot_sb = nullptr;
     size_t smem_rsb = 0;
+    // tensor-core rotation combine (ACQ_OPT_ROTATION_PRECISION != FP32)
+    RotMmaFn rot_mma = nullptr;
+    size_t smem_mma = 0;
+    int rot_prec = ACQ_PREC_FP32;
+    int mma_scale_log2 = 127;   // 127: by input type
     int Wrsb = 8, threads_rsb = 256;
     // warp-per-column sign / rotation stage
     SearchFn search_warp = nullptr;
@@ -651,6 +658,17 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             const int W = P->Wsimple;
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
+        } else if (g.path == 2 && P->rot_mma) {
+            RotMmaParams rp{};
+            rp.T = P->T.as<float2>(); rp.spc = g.spc; rp.spc_eff = g.spc_eff; rp.bs = g.bs; rp.R = g.R;
+            rp.combos = P->combos; rp.use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            rp.first = first | (last ? 2 : 0); rp.twD = P->fftD.tw; rp.pats = P->pats.as<float>();
+            rp.slots = a.d_slots; rp.drift = dr; rp.acc = P->accb.as<float>(); rp.win = P->winb.as<uint16_t>();
+            int sl = P->mma_scale_log2;
+            if (sl == 127) sl = dtype == ACQ_CI16 ? -10 : dtype == ACQ_CI8 ? -2 : 0;
+            rp.scale = std::ldexp(1.0f, sl);
+            rp.err = P->errflag.as<int>();
+            P->rot_mma<<<dim3((g.spc + kRotMmaW - 1) / kRotMmaW, n), 256, P->smem_mma, st>>>(rp);
         } else if (g.path == 2 && P->rot_sb && !P->search_warp) {
             const int W = P->Wrsb;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
@@ -1205,6 +1223,33 @@ int acq_plan_reset_kernel_times(acq_plan* P) {
 int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* effective) {
     return guarded([&] {
         if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (option == ACQ_OPT_ROTATION_PRECISION) {
+            if (value < ACQ_PREC_FP32 || value > ACQ_PREC_BF16_SPLIT)
+                throw AcqError(ACQ_ERR_ARGUMENT, "unknown precision " + std::to_string(value));
+            const Geometry& g = P->g;
+            RotMmaFn fn = nullptr;
+            size_t smem = 0;
+            const int n_cand = g.R * (1 << (g.ndb - 1));
+            if (value != ACQ_PREC_FP32 && g.path == 2 && g.n_be == 1 && n_cand <= 32 && !getenv_flag("ACQ_GENERIC_FFT"))
+                fn = pick_rot_mma(g.n_coh, g.nb, n_cand, static_cast<int>(value), &smem);
+            if (fn) {
+                set_smem((const void*)fn, smem);
+                P->errflag.ensure(sizeof(int));
+                CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
+            }
+            P->rot_mma = fn;
+            P->smem_mma = smem;
+            P->rot_prec = fn ? static_cast<int>(value) : ACQ_PREC_FP32;
+            if (effective) *effective = P->rot_prec;
+            return;
+        }
+        if (option == ACQ_OPT_MMA_SCALE_LOG2) {
+            if (value != 127 && (value < -64 || value > 64))
+                throw AcqError(ACQ_ERR_ARGUMENT, "scale exponent must be in -64:64 (or 127 for the default)");
+            P->mma_scale_log2 = static_cast<int>(value);
+            if (effective) *effective = value;
+            return;
+        }
         if (option != ACQ_OPT_FORM) throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
         if (value != ACQ_FORM_FUSED && value != ACQ_FORM_PLAIN)
             throw AcqError(ACQ_ERR_ARGUMENT, "unknown form " + std::to_string(value));

@@ -485,6 +485,9 @@ def main():
                     help="kernel form of the headline measurement (the other form is reported beside it)")
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS),
                     help="workload (cfg2, the reference's weak-signal search, is the headline)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "bf16", "fp16_split", "bf16_split"],
+                    help="rotation-combine arithmetic of the headline measurement on rotation-search workloads")
+    ap.add_argument("--no-precision-study", action="store_true")
     ap.add_argument("--accumulations", type=int, default=None,
                     help="non-coherent accumulations (profiling cases only; default: the workload's)")
     args = ap.parse_args()
@@ -521,6 +524,7 @@ def main():
                           num_coherently_integrated_code_periods=N_COH, bit_edge_search_steps=CFG["n_be"],
                           num_noncoherent_accumulations=n_nc, device=local_rank)
     main_form = plan.set_form(args.form)
+    main_prec = plan.set_rotation_precision(args.precision)
     other_form = "plain" if main_form == "fused" else "fused"
     if np.iscomplexobj(ci16):
         host = torch.from_numpy(ci16.view(np.float32).reshape(-1, 2)).pin_memory()
@@ -610,6 +614,44 @@ def main():
     ktimes = plan.kernel_times()
     plan.set_kernel_timing(False)
 
+    # ---- rotation searches: the combine on the tensor cores (FP16/BF16, single or split hi + lo)
+    # against the FP32 path: throughput, power error relative to the FP32 surface's peak on
+    # two PRNs (strongest planted, one absent) and agreement of every PRN's decisions
+    study = None
+    if plan.geometry.path == 2 and not args.no_precision_study:
+        study = {}
+        base_prec = main_prec
+        strong = max(sats, key=lambda s_: s_.cn0).prn
+        absent = next(p_ for p_ in PRNS if p_ not in {s_.prn for s_ in sats})
+        pair = [strong, absent]
+        plan.set_rotation_precision("fp32")
+        ref_all = A.acquire_device(plan, dev, PRNS)
+        ref_pb = {r.prn: np.asarray(r.power_bins, dtype=np.float64)
+                  for r in A.acquire_b(plan, host_np, pair, store_power_bins=True)}
+        for prec in ("fp32", "fp16", "bf16", "fp16_split", "bf16_split"):
+            if plan.set_rotation_precision(prec) != prec:
+                continue
+            A.acquire_device(plan, dev, PRNS)
+            pm = []
+            for _ in range(args.steps):
+                flush_l2()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(pstream)
+                A.acquire_device_async(plan, dev, PRNS)
+                e1.record(pstream)
+                out = A.fetch_results(plan, PRNS)
+                pm.append(e0.elapsed_time(e1))
+            same = sum(int(A.is_detected(a) == A.is_detected(b) and (not A.is_detected(b) or (
+                a.peak_doppler_bin, a.peak_code_bin, a.secondary_code_phase) == (
+                b.peak_doppler_bin, b.peak_code_bin, b.secondary_code_phase))) for a, b in zip(out, ref_all))
+            pb = {r.prn: np.asarray(r.power_bins, dtype=np.float64)
+                  for r in A.acquire_b(plan, host_np, pair, store_power_bins=True)}
+            err = max(float(np.max(np.abs(pb[q] - ref_pb[q])) / np.max(ref_pb[q])) for q in pair)
+            study[prec] = {"value": world * 1e3 / statistics.mean(pm), "unit": "acq/s",
+                           "max_power_error_vs_fp32": err, "prns_with_same_decisions": same}
+        plan.set_rotation_precision(base_prec)
+
     # ---- e2e: public API, pinned host input, H2D + compute + D2H inside the timed region
     e2e_s = []
     for _ in range(args.steps):
@@ -686,7 +728,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, CI16)",
             "config": {"workload": WORKLOAD if n_nc == N_NC else f"{WORKLOAD}_nnc{n_nc}", "prns": n_prn, "samples": samples, "num_doppler_bins": ndop,
-                       "samples_per_code": spc, "fft_size": F, "form": form,
+                       "samples_per_code": spc, "fft_size": F, "form": form, "rotation_precision": main_prec,
                        "l2": "flushed (256 MB write) before every timed step"},
             "msample_prn_per_s": value * n_prn * samples / 1e6,
             "other_form": {"form": other_form, "value": plain_value, "unit": "acq/s",
@@ -696,7 +738,7 @@ def main():
                     "d2h_bytes_per_step": n_prn * 72, "ms_per_step": t_e2e * 1e3},
             "gpu_launches": int(launches_per_step * args.steps),
             "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "detected_prns": det, "planted_prns": [s.prn for s in sats]}
+            "detected_prns": det, "planted_prns": [s.prn for s in sats], "precision_study": study}
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

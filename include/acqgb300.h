@@ -159,10 +159,22 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_OPT_FORM 0               /* ACQ_FORM_PLAIN (default) or ACQ_FORM_FUSED */
 #define ACQ_FORM_FUSED 0             /* cluster kernel: tile + Doppler stage + accumulation in shared memory */
 #define ACQ_FORM_PLAIN 1             /* one kernel per stage, coherent tile and accumulator in HBM */
+#define ACQ_OPT_ROTATION_PRECISION 1 /* arithmetic of the secondary-code rotation combine: */
+#define ACQ_PREC_FP32 0              /*   FP32 FFTs on the CUDA cores (default) */
+#define ACQ_PREC_FP16 1              /*   tensor cores, FP16 sub-block spectra, FP32 accumulation */
+#define ACQ_PREC_BF16 2              /*   tensor cores, BF16 sub-block spectra */
+#define ACQ_PREC_FP16_SPLIT 3        /*   tensor cores, spectra split hi + lo in FP16 (two MMAs) */
+#define ACQ_PREC_BF16_SPLIT 4        /*   tensor cores, spectra split hi + lo in BF16 (two MMAs) */
+#define ACQ_OPT_MMA_SCALE_LOG2 2     /* power-of-two scale of the spectra before FP16 rounding (default: by
+                                        input type, CF32/CF64 0, CI16 -10, CI8 -2) */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
- * form is used only where the plan's sizes have a fused kernel (otherwise plain). Returns the
- * form now in effect through `effective` (may be NULL). No reference counterpart. */
+ * form is used only where the plan's sizes have a fused kernel (otherwise plain).
+ * ACQ_OPT_ROTATION_PRECISION selects the rotation combine's arithmetic on plans with a
+ * secondary-code rotation search; a tensor-core variant is used where the plan's geometry has
+ * one (one bit-edge step, at most 32 candidates), otherwise FP32. ACQ_OPT_MMA_SCALE_LOG2 sets
+ * the spectra scale (values -64..64; 127 restores the per-input-type default). Returns the
+ * value now in effect through `effective` (may be NULL). No reference counterpart. */
 int acq_plan_set_option(acq_plan* plan, int32_t option, int64_t value, int64_t* effective);
 
 /* Kernel classes for per-launch device timing. */
