@@ -34,7 +34,7 @@ struct RotMmaParams;
 using RotMmaFn = void (*)(RotMmaParams);
 // tensor-core rotation combine for (coherent periods, blocks per period, candidates) at an
 // ACQ_PREC_* precision other than FP32; nullptr when not instantiated; *smem = dynamic bytes.
-RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int prec, size_t* smem);
+RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec, size_t* smem);
 
 using SearchFn = void (*)(SearchParams);
 // warp-per-column search stage (mode 1 sign, 2 rotation); pc = candidates transformed together

@@ -6,26 +6,26 @@
 namespace acq {
 
 namespace {
-template <int NC, int NB, int QP>
+template <int NC, int NB, int QP, int CB>
 RotMmaFn pick_prec(int prec, size_t* smem) {
     using S = RotMmaShape<NC, NB, QP>;
     switch (prec) {
-        case ACQ_PREC_FP16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, 0, 1>;
-        case ACQ_PREC_BF16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, 1, 1>;
-        case ACQ_PREC_FP16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, 0, 2>;
-        case ACQ_PREC_BF16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, 1, 2>;
+        case ACQ_PREC_FP16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, CB, 0, 1>;
+        case ACQ_PREC_BF16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, CB, 1, 1>;
+        case ACQ_PREC_FP16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, CB, 0, 2>;
+        case ACQ_PREC_BF16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, CB, 1, 2>;
         default: return nullptr;
     }
 }
 }  // namespace
 
-#define ACQ_MMA_CASE(NC, NB, QP) \
-    if (n_coh == NC && nb == NB && qp == QP) return pick_prec<NC, NB, QP>(prec, smem);
+#define ACQ_MMA_CASE(NC, NB, QP, CB) \
+    if (n_coh == NC && nb == NB && qp == QP && combos == CB) return pick_prec<NC, NB, QP, CB>(prec, smem);
 
-RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int prec, size_t* smem) {
+RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec, size_t* smem) {
     const int qp = (n_candidates + 7) / 8 * 8;
-    ACQ_MMA_CASE(20, 25, 24) ACQ_MMA_CASE(10, 20, 16) ACQ_MMA_CASE(20, 12, 24) ACQ_MMA_CASE(10, 16, 16)
-    ACQ_MMA_CASE(10, 4, 16) ACQ_MMA_CASE(20, 20, 24)
+    ACQ_MMA_CASE(20, 25, 24, 2) ACQ_MMA_CASE(10, 20, 16, 1) ACQ_MMA_CASE(20, 12, 24, 2) ACQ_MMA_CASE(10, 16, 16, 1)
+    ACQ_MMA_CASE(10, 4, 16, 1) ACQ_MMA_CASE(20, 20, 24, 2)
     return nullptr;
 }
 

@@ -146,8 +146,9 @@ struct RotMmaShape {
     __host__ __device__ static constexpr int smem_bytes(int nsplit) { return off_bar(nsplit) + 16 + 1024; }   // + alignment slack
 };
 
-template <int NC, int NB, int QP, int FMT, int NSPLIT>
+template <int NC, int NB, int QP, int CB, int FMT, int NSPLIT>
 __global__ void __launch_bounds__(256, 2) k_rot_mma(RotMmaParams p) {
+    static_assert(CB == 1 || CB == 2 || CB == 4 || CB == 8, "data-bit combinations per rotation");
     using S = RotMmaShape<NC, NB, QP>;
     constexpr int W = S::W, ND = S::ND, KCH = S::KCH, MT = S::MT;
     extern __shared__ uint8_t smraw_[];
@@ -285,14 +286,14 @@ __global__ void __launch_bounds__(256, 2) k_rot_mma(RotMmaParams p) {
                     tc_ld8(tb + 8 * j, re);
                     tc_ld8(tb + QP + 8 * j, im);
                     tc_wait_ld();
-                    // max over each group of `combos` candidates (a power of two dividing 8)
+                    // max over each group of CB data-bit combinations (CB divides 8)
                     float bestv[8];
                     int bwv[8];
                     bool keep[8];
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int q = 8 * j + i;
-                        const int d = q & (p.combos - 1);
+                        const int d = q & (CB - 1);
                         const float pw = __fadd_rn(__fmul_rn(re[i], re[i]), __fmul_rn(im[i], im[i])) * inv_s2;
                         if (d == 0) {
                             best = 0.f;
@@ -304,19 +305,19 @@ __global__ void __launch_bounds__(256, 2) k_rot_mma(RotMmaParams p) {
                         }
                         bestv[i] = best;
                         bwv[i] = bw;
-                        keep[i] = valid && d == p.combos - 1 && q / p.combos < p.R;
+                        keep[i] = valid && d == CB - 1 && q / CB < p.R;
                     }
                     // accumulator read-modify-write: the chunk's loads first, then its stores
                     float old[8];
                     if (!(p.first & 1)) {
 #pragma unroll
                         for (int i = 0; i < 8; ++i)
-                            old[i] = keep[i] ? ap[rbase + ((8 * j + i) / p.combos) * p.spc] : 0.f;
+                            old[i] = keep[i] ? ap[rbase + ((8 * j + i) / CB) * p.spc] : 0.f;
                     }
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         if (keep[i]) {
-                            const int64_t idx = rbase + ((8 * j + i) / p.combos) * p.spc;
+                            const int64_t idx = rbase + ((8 * j + i) / CB) * p.spc;
                             ap[idx] = (p.first & 1) ? bestv[i] : old[i] + bestv[i];
                             if (p.first & 2) wp[idx] = static_cast<uint16_t>(bwv[i]);
                         }

@@ -1231,7 +1231,7 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             size_t smem = 0;
             const int n_cand = g.R * (1 << (g.ndb - 1));
             if (value != ACQ_PREC_FP32 && g.path == 2 && g.n_be == 1 && n_cand <= 32 && !getenv_flag("ACQ_GENERIC_FFT"))
-                fn = pick_rot_mma(g.n_coh, g.nb, n_cand, static_cast<int>(value), &smem);
+                fn = pick_rot_mma(g.n_coh, g.nb, n_cand, 1 << (g.ndb - 1), static_cast<int>(value), &smem);
             if (fn) {
                 set_smem((const void*)fn, smem);
                 P->errflag.ensure(sizeof(int));
