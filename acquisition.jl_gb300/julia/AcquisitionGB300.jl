@@ -1,0 +1,248 @@
+# AcquisitionGB300.jl — Julia binding of libacqgb300 (the C ABI in include/acqgb300.h).
+#
+# Mirrors Acquisition.jl's public API for the FM-DBZP path (plan_acquire src/plan.jl:312-324,
+# acquire! src/acquire.jl:54-61,788-797, acquire :838-882, AcquisitionResults
+# src/Acquisition.jl:81-109, is_detected / get_num_cells :124-142, cfar_threshold
+# src/cfar.jl:64-85) on top of `ccall`, plus the ragged-batch, precision and continuous-correlator
+# extensions. The correlator's power has a ChainRulesCore `rrule` whose pullback calls the
+# adjoint kernel (the code replica is recomputed on the device, not stored).
+#
+# Requires: GNSSSignals, Unitful, CUDA (device arrays for the correlator), ChainRulesCore.
+# This environment has no Julia; the binding follows the header field by field.
+module AcquisitionGB300
+
+using GNSSSignals
+using Unitful: Hz, ustrip
+import ChainRulesCore
+using CUDA
+
+const lib = joinpath(@__DIR__, "..", "acqgb300", "libacqgb300.so")
+
+# ---- structs (layouts of include/acqgb300.h) ----
+struct PlanDesc
+    system::Int32
+    sampling_freq_hz::Float64
+    min_doppler_coverage_hz::Float64
+    num_coherently_integrated_code_periods::Int32
+    bit_edge_search_steps::Int32
+    num_noncoherent_accumulations::Int32
+    noise_estimator::Int32
+    use_secondary_code::Int32
+    max_secondary_code_rotations::Int32
+    device::Int32
+end
+
+struct CResult
+    prn::Int32
+    secondary_code_phase::Int32
+    carrier_doppler_hz::Float64
+    code_phase::Float64
+    cn0_dbhz::Float64
+    noise_power::Float32
+    peak_to_noise_ratio::Float32
+    peak_power::Float32
+    num_noncoherent_integrations::Int32
+    peak_doppler_bin::Int32
+    peak_code_bin::Int32
+    sign_pattern::Int32
+    bit_edge::Int32
+    detected::Int32
+    reserved::Int32
+end
+
+struct CorrCell
+    prn::Int32
+    reserved::Int32
+    code_phase::Float64
+    doppler_hz::Float64
+end
+
+struct CorrResult
+    power::Float64
+    grad::NTuple{2,Float64}
+    hess::NTuple{3,Float64}
+    z_re::Float64
+    z_im::Float64
+    iterations::Int32
+    status::Int32
+end
+
+function check(st)
+    st == 0 && return nothing
+    buf = Vector{UInt8}(undef, 4096)
+    ccall((:acq_last_error, lib), Cint, (Ptr{UInt8}, Csize_t), buf, length(buf))
+    msg = unsafe_string(pointer(buf))
+    st in (1, 2, 3) ? throw(ArgumentError(msg)) : error("libacqgb300 status $st: $msg")
+end
+
+sysid(::GPSL1CA) = Int32(0)
+sysid(::GPSL5I) = Int32(1)
+sysid(::GalileoE1B) = Int32(2)
+
+dtype(::Type{ComplexF32}) = Int32(0)
+dtype(::Type{Complex{Int16}}) = Int32(1)
+dtype(::Type{Complex{Int8}}) = Int32(2)
+dtype(::Type{ComplexF64}) = Int32(3)
+
+# ---- plan_acquire / acquire! / acquire ----
+struct OppositeRowNoiseEstimator end
+struct GlobalMeanNoiseEstimator end
+estid(::OppositeRowNoiseEstimator) = Int32(0)
+estid(::GlobalMeanNoiseEstimator) = Int32(1)
+
+mutable struct AcquisitionPlan
+    h::Ptr{Cvoid}
+    system::Any
+    sampling_freq::Float64
+    avail_prns::Vector{Int32}
+end
+
+function plan_acquire(system, sampling_freq, prns; min_doppler_coverage = 7000Hz,
+                      num_coherently_integrated_code_periods = 1, bit_edge_search_steps = 1,
+                      num_noncoherent_accumulations = 1, noise_estimator = OppositeRowNoiseEstimator(),
+                      use_secondary_code = true, max_secondary_code_rotations = 32, fft_flag = nothing,
+                      device = 0)
+    fs = Float64(ustrip(Hz, sampling_freq))
+    d = Ref(PlanDesc(sysid(system), fs, Float64(ustrip(Hz, min_doppler_coverage)),
+                     num_coherently_integrated_code_periods, bit_edge_search_steps,
+                     num_noncoherent_accumulations, estid(noise_estimator), use_secondary_code,
+                     max_secondary_code_rotations, device))
+    p = Int32.(collect(prns))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    # codes = C_NULL: the library's generators; pass GNSSSignals codes (n_prns x code length
+    # Int8) to use the package's chips bit for bit.
+    check(ccall((:acq_plan_create, lib), Cint, (Ref{PlanDesc}, Ptr{Int32}, Int32, Ptr{Int8}, Ref{Ptr{Cvoid}}),
+                d, p, length(p), C_NULL, h))
+    plan = AcquisitionPlan(h[], system, fs, p)
+    finalizer(pl -> ccall((:acq_plan_destroy, lib), Cint, (Ptr{Cvoid},), pl.h), plan)
+end
+
+struct AcquisitionResults
+    system::Any
+    prn::Int
+    sampling_frequency::Float64
+    carrier_doppler::Float64
+    code_phase::Float64
+    secondary_code_phase::Union{Int,Nothing}
+    CN0::Float64
+    noise_power::Float32
+    peak_to_noise_ratio::Float32
+    num_noncoherent_integrations::Int
+    power_bins::Union{Matrix{Float32},Nothing}
+end
+
+function acquire!(plan::AcquisitionPlan, signal::AbstractVector{T}, prns; interm_freq = 0.0Hz,
+                  subsample_interpolation = false, store_power_bins = false) where {T}
+    p = Int32.(collect(prns))
+    res = Vector{CResult}(undef, length(p))
+    flags = UInt32(subsample_interpolation) | (UInt32(store_power_bins) << 1)
+    check(ccall((:acq_acquire, lib), Cint,
+                (Ptr{Cvoid}, Ptr{T}, Int32, Int64, Ptr{Int32}, Int32, Float64, UInt32, Ptr{CResult}, Ptr{Float32}),
+                plan.h, signal, dtype(T), length(signal), p, length(p), Float64(ustrip(Hz, interm_freq)), flags,
+                res, C_NULL))
+    [AcquisitionResults(plan.system, r.prn, plan.sampling_freq, r.carrier_doppler_hz, r.code_phase,
+                        r.secondary_code_phase < 0 ? nothing : Int(r.secondary_code_phase), r.cn0_dbhz,
+                        r.noise_power, r.peak_to_noise_ratio, r.num_noncoherent_integrations, nothing) for r in res]
+end
+
+acquire(system, signal, sampling_freq, prns; kw...) =
+    acquire!(plan_acquire(system, sampling_freq, prns), signal, prns; kw...)
+
+function cfar_threshold(pfa, num_cells; num_noncoherent_integrations = 1)
+    out = Ref{Float64}(0)
+    check(ccall((:acq_cfar_threshold, lib), Cint, (Float64, Int64, Int32, Ref{Float64}), pfa, num_cells,
+                num_noncoherent_integrations, out))
+    out[]
+end
+
+# ---- tensor-core precision option ----
+const PRECISIONS = Dict(:fp32 => 0, :fp16 => 1, :bf16 => 2, :fp16_split => 3, :bf16_split => 4)
+
+function set_rotation_precision!(plan::AcquisitionPlan, prec::Symbol)
+    eff = Ref{Int64}(0)
+    check(ccall((:acq_plan_set_option, lib), Cint, (Ptr{Cvoid}, Int32, Int64, Ref{Int64}), plan.h, 1,
+                PRECISIONS[prec], eff))
+    only(k for (k, v) in PRECISIONS if v == eff[])
+end
+
+# ---- continuous correlator ----
+mutable struct Correlator
+    h::Ptr{Cvoid}
+    system::Any
+    sampling_freq::Float64
+end
+
+function Correlator(system, sampling_freq, prns)
+    p = Int32.(collect(prns))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:acq_corr_create, lib), Cint, (Int32, Float64, Ptr{Int32}, Int32, Ptr{Int8}, Ref{Ptr{Cvoid}}),
+                sysid(system), Float64(ustrip(Hz, sampling_freq)), p, length(p), C_NULL, h))
+    c = Correlator(h[], system, Float64(ustrip(Hz, sampling_freq)))
+    finalizer(x -> ccall((:acq_corr_destroy, lib), Cint, (Ptr{Cvoid},), x.h), c)
+end
+
+stream_ptr() = CUDA.stream().handle
+
+function correlator_eval(c::Correlator, x::CuVector{ComplexF32}, cells::CuVector{CorrCell}; hessian = false)
+    out = CuVector{CorrResult}(undef, length(cells))
+    check(ccall((:acq_corr_eval, lib), Cint,
+                (Ptr{Cvoid}, CuPtr{ComplexF32}, Int32, Int64, Float64, CuPtr{CorrCell}, Int32, Int32,
+                 CuPtr{CorrResult}, Ptr{Cvoid}),
+                c.h, x, 0, length(x), 0.0, cells, length(cells), hessian, out, stream_ptr()))
+    out
+end
+
+function correlator_vjp(c::Correlator, n, cells::CuVector{CorrCell}, zbar::CuVector{ComplexF32})
+    xbar = CuVector{ComplexF32}(undef, n)
+    check(ccall((:acq_corr_vjp_samples, lib), Cint,
+                (Ptr{Cvoid}, Int64, Float64, CuPtr{CorrCell}, CuPtr{ComplexF32}, Int32, CuPtr{ComplexF32}, Ptr{Cvoid}),
+                c.h, n, 0.0, cells, zbar, length(cells), xbar, stream_ptr()))
+    xbar
+end
+
+"""
+    correlator_power(c, x, prns, code_phases, dopplers) -> Vector{Float64}
+
+P = |z|^2 per cell (src/generate_test_signal.jl:45-68's correlation at continuous code phase
+and Doppler). Differentiable: see the `rrule` below.
+"""
+function correlator_power(c::Correlator, x::CuVector{ComplexF32}, prns, tau::AbstractVector, f::AbstractVector)
+    cells = CuVector(CorrCell.(Int32.(prns), Int32(0), Float64.(tau), Float64.(f)))
+    r = Array(correlator_eval(c, x, cells))
+    [q.power for q in r]
+end
+
+function ChainRulesCore.rrule(::typeof(correlator_power), c::Correlator, x::CuVector{ComplexF32}, prns, tau, f)
+    cells = CuVector(CorrCell.(Int32.(prns), Int32(0), Float64.(tau), Float64.(f)))
+    r = Array(correlator_eval(c, x, cells))
+    P = [q.power for q in r]
+    function pullback(Pbar)
+        pb = collect(Float64, ChainRulesCore.unthunk(Pbar))
+        # z-bar = 2 P-bar z ; the kernel recomputes the replica for x-bar
+        zbar = CuVector(ComplexF32.(2 .* pb .* [complex(q.z_re, q.z_im) for q in r]))
+        xbar = correlator_vjp(c, length(x), cells, zbar)
+        taubar = pb .* [q.grad[1] for q in r]
+        fbar = pb .* [q.grad[2] for q in r]
+        (ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), xbar, ChainRulesCore.NoTangent(), taubar, fbar)
+    end
+    P, pullback
+end
+
+"""
+    refine!(c, x, cells; max_iterations = 20, tol_chips = 1e-4, tol_hz = 1e-3,
+            max_step_chips = 0.25, max_step_hz = 0.25 * fs / length(x))
+
+Batched Newton refinement of every cell in place (beside the grid's parabolic interpolation).
+"""
+function refine!(c::Correlator, x::CuVector{ComplexF32}, cells::CuVector{CorrCell}; max_iterations = 20,
+                 tol_chips = 1e-4, tol_hz = 1e-3, max_step_chips = 0.25, max_step_hz = 0.25 * c.sampling_freq / length(x))
+    out = CuVector{CorrResult}(undef, length(cells))
+    check(ccall((:acq_corr_refine, lib), Cint,
+                (Ptr{Cvoid}, CuPtr{ComplexF32}, Int32, Int64, Float64, CuPtr{CorrCell}, Int32, Int32, Float64,
+                 Float64, Float64, Float64, CuPtr{CorrResult}, Ptr{Cvoid}),
+                c.h, x, 0, length(x), 0.0, cells, length(cells), max_iterations, tol_chips, tol_hz,
+                max_step_chips, max_step_hz, out, stream_ptr()))
+    out
+end
+
+end # module
