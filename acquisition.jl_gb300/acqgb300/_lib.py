@@ -76,10 +76,13 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_plan_reset_kernel_times", "acq_est_signal_noise_power_noalloc", "acq_plan_set_option",
             "acq_batch_create", "acq_batch_destroy", "acq_batch_input_ptr", "acq_batch_upload", "acq_batch_launch",
             "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
-            "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine"]
+            "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine",
+            "acq_plan_get_option"]
 ACQ_OPT_FORM = 0
 ACQ_OPT_ROTATION_PRECISION = 1
 ACQ_OPT_MMA_SCALE_LOG2 = 2
+ACQ_OPT_TILE_THREADS, ACQ_OPT_TILE_BLOCKS, ACQ_OPT_TILE_PAD = 3, 4, 5
+ACQ_OPT_COLUMN_WIDTH, ACQ_OPT_COLUMN_CTAS_PER_SM = 6, 7
 ACQ_FORM_FUSED, ACQ_FORM_PLAIN = 0, 1
 KERNEL_KINDS = 8
 KERNEL_NAMES = ["frontend", "tile", "column", "stats", "extract", "secondary", "fused", "k7"]
@@ -122,6 +125,7 @@ def load():
     lib.acq_est_signal_noise_power_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_double,
                                                        C.c_int32, C.c_void_p, C.c_void_p]
     lib.acq_plan_set_option.argtypes = [P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
+    lib.acq_plan_get_option.argtypes = [P, C.c_int32, C.POINTER(C.c_int64)]
     lib.acq_corr_create.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int8),
                                     C.POINTER(P)]
     lib.acq_corr_destroy.argtypes = [P]

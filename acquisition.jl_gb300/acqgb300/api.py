@@ -240,6 +240,17 @@ class AcquisitionPlan:
         _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_FORM, val, C.byref(eff)))
         return "fused" if eff.value == L.ACQ_FORM_FUSED else "plain"
 
+    def set_option(self, option: int, value: int) -> int:
+        """acq_plan_set_option: returns the value in effect (see include/acqgb300.h)."""
+        eff = C.c_int64()
+        _check(L.load().acq_plan_set_option(self._h, int(option), int(value), C.byref(eff)))
+        return eff.value
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int64()
+        _check(L.load().acq_plan_get_option(self._h, int(option), C.byref(v)))
+        return v.value
+
     def set_rotation_precision(self, precision: str) -> str:
         """Arithmetic of the secondary-code rotation combine: 'fp32' (FFTs on the CUDA cores, the
         default) or a tensor-core variant 'fp16', 'bf16', 'fp16_split', 'bf16_split' (sub-block

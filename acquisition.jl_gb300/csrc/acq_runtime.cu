@@ -184,7 +184,8 @@ struct acq_plan {
     ColTmaFn col_tma = nullptr;
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
-    int tmaW = 16, tmaBoxRows = 1, tmaBoxes = 1, tmaGrid = 1, tmaH = 0;
+    int tmaW = 16, tmaBoxRows = 1, tmaBoxes = 1, tmaGrid = 1, tmaH = 0, tmaCtasPerSm = 0;
+    int n_plan_prns = 0;
     size_t smem_col_tma = 0;
     // fused cluster form
     FusedFn fused = nullptr;
@@ -296,7 +297,7 @@ void setup_fused(acq_plan* P) {
 }
 
 // TMA-staged column stage: T for all steps in HBM, a tensor map over it, a persistent grid.
-void setup_col_tma(acq_plan* P, int n_prns) {
+void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     const Geometry& g = P->g;
     P->col_tma = nullptr;
     if (g.path != 0 || !P->tile_fs || getenv_flag("ACQ_GENERIC_FFT") || getenv_flag("ACQ_NO_TMA")) return;
@@ -314,7 +315,6 @@ void setup_col_tma(acq_plan* P, int n_prns) {
         code_drift_shifts(g, *P->sys, P->desc.sampling_freq_hz, m, dr.data());
         for (int v : dr) H = std::max(H, std::min(v, g.spc - v));
     }
-    const int W = 16;
     if (H > W) return;
     int box = 1;
     for (int d = 1; d <= 256 && d <= g.ndop; ++d)
@@ -350,7 +350,8 @@ void setup_col_tma(acq_plan* P, int n_prns) {
     P->tmaW = W;
     P->tmaBoxRows = box;
     P->tmaBoxes = g.ndop / box;
-    P->tmaGrid = sms * per_sm;
+    P->tmaGrid = sms * (ctas_per_sm > 0 ? std::min(per_sm, ctas_per_sm) : per_sm);
+    P->tmaCtasPerSm = ctas_per_sm > 0 ? std::min(per_sm, ctas_per_sm) : per_sm;
     P->tmaH = H;
     P->smem_col_tma = smem;
 }
@@ -447,6 +448,7 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     }
     P->nct = (g.spc_eff + kStatsCols - 1) / kStatsCols;
     setup_fused(P);
+    P->n_plan_prns = n_prns;
     setup_col_tma(P, n_prns);
 
     // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
@@ -1220,6 +1222,23 @@ int acq_plan_reset_kernel_times(acq_plan* P) {
     });
 }
 
+int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
+    return guarded([&] {
+        if (!P || !value) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        switch (option) {
+            case ACQ_OPT_FORM: *value = (P->fused && P->form == ACQ_FORM_FUSED) ? ACQ_FORM_FUSED : ACQ_FORM_PLAIN; break;
+            case ACQ_OPT_ROTATION_PRECISION: *value = P->rot_prec; break;
+            case ACQ_OPT_MMA_SCALE_LOG2: *value = P->mma_scale_log2; break;
+            case ACQ_OPT_TILE_THREADS: *value = P->tile_fs ? P->tileThreads : 0; break;
+            case ACQ_OPT_TILE_BLOCKS: *value = P->tile_fs ? P->tileNF : 0; break;
+            case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->g.fft_size : 0; break;
+            case ACQ_OPT_COLUMN_WIDTH: *value = P->col_tma ? P->tmaW : 0; break;
+            case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_tma ? P->tmaCtasPerSm : 0; break;
+            default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
+        }
+    });
+}
+
 int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* effective) {
     return guarded([&] {
         if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
@@ -1241,6 +1260,53 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             P->smem_mma = smem;
             P->rot_prec = fn ? static_cast<int>(value) : ACQ_PREC_FP32;
             if (effective) *effective = P->rot_prec;
+            return;
+        }
+        if (option == ACQ_OPT_TILE_THREADS || option == ACQ_OPT_TILE_BLOCKS || option == ACQ_OPT_TILE_PAD) {
+            const Geometry& g = P->g;
+            if (!P->tile_fs) {
+                if (effective) *effective = 0;
+                return;
+            }
+            CK(cudaStreamSynchronize(P->stream));
+            if (option == ACQ_OPT_TILE_THREADS) {
+                if (value < 32 || value > 256 || value % 32) throw AcqError(ACQ_ERR_ARGUMENT, "tile threads must be 32..256, a multiple of 32");
+                P->tileThreads = static_cast<int>(value);
+            } else if (option == ACQ_OPT_TILE_BLOCKS) {
+                if (value < 1 || value > g.nb) throw AcqError(ACQ_ERR_ARGUMENT, "tile blocks per CTA must be in 1:num_blocks");
+                P->tileNF = static_cast<int>(value);
+            } else {
+                if (value < 0 || value > 32) throw AcqError(ACQ_ERR_ARGUMENT, "tile padding must be in 0:32");
+                P->tileFS = g.fft_size + static_cast<int>(value);
+            }
+            const size_t smem = sizeof(float2) * (g.fft_size + (size_t)P->tileFS * P->tileNF);
+            if (smem > 200 * 1024) throw AcqError(ACQ_ERR_ARGUMENT, "tile configuration exceeds shared memory");
+            P->smem_tile_fs = smem;
+            set_smem((const void*)P->tile_fs, P->smem_tile_fs);
+            if (effective)
+                *effective = option == ACQ_OPT_TILE_THREADS ? P->tileThreads
+                           : option == ACQ_OPT_TILE_BLOCKS  ? P->tileNF
+                                                            : P->tileFS - g.fft_size;
+            return;
+        }
+        if (option == ACQ_OPT_COLUMN_WIDTH || option == ACQ_OPT_COLUMN_CTAS_PER_SM) {
+            if (!P->col_tma) {
+                if (effective) *effective = 0;
+                return;
+            }
+            CK(cudaStreamSynchronize(P->stream));
+            int W = P->tmaW, cps = P->tmaCtasPerSm;
+            if (option == ACQ_OPT_COLUMN_WIDTH) {
+                if (value != 8 && value != 16 && value != 32) throw AcqError(ACQ_ERR_ARGUMENT, "column width must be 8, 16 or 32");
+                W = static_cast<int>(value);
+            } else {
+                if (value < 1 || value > 32) throw AcqError(ACQ_ERR_ARGUMENT, "CTAs per SM must be in 1:32");
+                cps = static_cast<int>(value);
+            }
+            const int oldW = P->tmaW, oldc = P->tmaCtasPerSm;
+            setup_col_tma(P, P->n_plan_prns, W, cps);
+            if (!P->col_tma) setup_col_tma(P, P->n_plan_prns, oldW, oldc);   // keep the previous shape
+            if (effective) *effective = option == ACQ_OPT_COLUMN_WIDTH ? P->tmaW : P->tmaCtasPerSm;
             return;
         }
         if (option == ACQ_OPT_MMA_SCALE_LOG2) {

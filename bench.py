@@ -488,6 +488,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "bf16", "fp16_split", "bf16_split"],
                     help="rotation-combine arithmetic of the headline measurement on rotation-search workloads")
     ap.add_argument("--no-precision-study", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default launch shapes (otherwise the autotuner picks them before timing)")
     ap.add_argument("--accumulations", type=int, default=None,
                     help="non-coherent accumulations (profiling cases only; default: the workload's)")
     args = ap.parse_args()
@@ -538,6 +540,13 @@ def main():
     def flush_l2():
         flush.zero_()
         torch.cuda.synchronize()
+
+    # launch shapes from the project's autotuner (tile / column CTA shapes; results unchanged)
+    tuned = None
+    if not args.no_autotune:
+        from acqgb300 import autotune as T
+        tuned = T.tune(plan, dev, PRNS, reps=3, passes=1, store=False,
+                       knobs=("tile_threads", "tile_blocks", "tile_pad", "column_width", "column_ctas_per_sm"))
 
     # warm-up (device-resident and public API)
     for _ in range(args.warmup):
@@ -729,6 +738,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, CI16)",
             "config": {"workload": WORKLOAD if n_nc == N_NC else f"{WORKLOAD}_nnc{n_nc}", "prns": n_prn, "samples": samples, "num_doppler_bins": ndop,
                        "samples_per_code": spc, "fft_size": F, "form": form, "rotation_precision": main_prec,
+                       "launch_shapes": (dict(tuned["settings"], tuned_ms=tuned["ms"], default_ms=tuned["start_ms"])
+                                         if tuned else "defaults"),
                        "l2": "flushed (256 MB write) before every timed step"},
             "msample_prn_per_s": value * n_prn * samples / 1e6,
             "other_form": {"form": other_form, "value": plain_value, "unit": "acq/s",

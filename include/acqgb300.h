@@ -167,15 +167,26 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_PREC_BF16_SPLIT 4        /*   tensor cores, spectra split hi + lo in BF16 (two MMAs) */
 #define ACQ_OPT_MMA_SCALE_LOG2 2     /* power-of-two scale of the spectra before FP16 rounding (default: by
                                         input type, CF32/CF64 0, CI16 -10, CI8 -2) */
+/* Launch shapes (the autotuner's knobs; `effective` = the value in effect, 0 where the plan's
+ * sizes have no such kernel): */
+#define ACQ_OPT_TILE_THREADS 3       /* coherent-tile kernel: threads per CTA (32..256, multiple of 32) */
+#define ACQ_OPT_TILE_BLOCKS 4        /*   code blocks (inverse FFTs) per CTA round (1..num_blocks) */
+#define ACQ_OPT_TILE_PAD 5           /*   shared-memory padding between FFT buffers, complex elements (0..32) */
+#define ACQ_OPT_COLUMN_WIDTH 6       /* TMA column kernel: code-phase columns per tile (8, 16, 32) */
+#define ACQ_OPT_COLUMN_CTAS_PER_SM 7 /*   persistent CTAs per SM (1..occupancy limit) */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
  * form is used only where the plan's sizes have a fused kernel (otherwise plain).
  * ACQ_OPT_ROTATION_PRECISION selects the rotation combine's arithmetic on plans with a
  * secondary-code rotation search; a tensor-core variant is used where the plan's geometry has
  * one (one bit-edge step, at most 32 candidates), otherwise FP32. ACQ_OPT_MMA_SCALE_LOG2 sets
- * the spectra scale (values -64..64; 127 restores the per-input-type default). Returns the
- * value now in effect through `effective` (may be NULL). No reference counterpart. */
+ * the spectra scale (values -64..64; 127 restores the per-input-type default). The launch-shape
+ * options wait for the plan's stream and apply to later acquisitions (batches keep the shapes
+ * they were captured with). Returns the value now in effect through `effective` (may be NULL).
+ * No reference counterpart. */
 int acq_plan_set_option(acq_plan* plan, int32_t option, int64_t value, int64_t* effective);
+/* Read the value of a plan option now in effect (0 for a launch shape the plan's sizes lack). */
+int acq_plan_get_option(const acq_plan* plan, int32_t option, int64_t* value);
 
 /* Kernel classes for per-launch device timing. */
 #define ACQ_KERNEL_FRONTEND 0        /* downconversion + double-block FFT */

@@ -1,0 +1,30 @@
+"""CPU checks of the autotuner's search and cache (no GPU)."""
+import itertools
+import json
+
+from acqgb300 import autotune as T
+
+
+def test_coordinate_descent_finds_separable_minimum():
+    space = {"a": [1, 2, 3, 4], "b": [8, 16, 32], "c": ["x", "y"]}
+    target = {"a": 3, "b": 16, "c": "y"}
+    cost = lambda s: (s["a"] - 3) ** 2 + abs(s["b"] - 16) / 8 + (0 if s["c"] == "y" else 1) + 1.0
+    best, c, trials = T.coordinate_descent(cost, {"a": 1, "b": 32, "c": "x"}, space)
+    assert best == target and c == 1.0
+    full = len(list(itertools.product(*space.values())))
+    assert len(trials) < full
+
+
+def test_coordinate_descent_keeps_start_when_nothing_improves():
+    best, c, trials = T.coordinate_descent(lambda s: 5.0, {"a": 1}, {"a": [1, 2, 3]})
+    assert best == {"a": 1} and c == 5.0 and len(trials) == 3
+
+
+def test_cache_round_trip(tmp_path):
+    p = str(tmp_path / "sub" / "cache.json")
+    assert T.load_cache(p) == {}
+    T.save_cache({"k": {"settings": {"tile_threads": 128}, "ms": 1.5}}, p)
+    assert T.load_cache(p)["k"]["settings"]["tile_threads"] == 128
+    (tmp_path / "bad.json").write_text("{not json")
+    assert T.load_cache(str(tmp_path / "bad.json")) == {}
+    json.loads(open(p).read())
