@@ -30,6 +30,12 @@ using RotSbFn = void (*)(const float2*, int, const float2*, const float*, int, i
 // *w = columns per block, *threads = block size.
 RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads);
 
+using SignSbFn = void (*)(const float2*, int, const float2*, const float*, int, int, int, const int*, const int*, int,
+                          float*, uint16_t*, int);
+// data-bit / bit-edge search split by sub-blocks for (ndop, data bits); nullptr when not
+// instantiated. *w = columns per block, *threads = block size, *smem = dynamic bytes.
+SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem);
+
 struct RotMmaParams;
 using RotMmaFn = void (*)(RotMmaParams);
 // tensor-core rotation combine for (coherent periods, blocks per period, candidates) at an

@@ -48,6 +48,20 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
     return nullptr;
 }
 
+#define ACQ_SSB_CASE(N1, N2, W, NDB)                                                                 \
+    if (ndop == N1 * N2 && ndb == NDB) {                                                              \
+        *w = W;                                                                                      \
+        *threads = (1 << (NDB - 1)) * N1 * W;                                                         \
+        *smem = sizeof(float2) * ((size_t)(1 + NDB) * N1 * N2 * W + N1 * N2) + 64;                    \
+        return &k_col_sign_sb<N1, N2, W, NDB>;                                                        \
+    }
+
+SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {
+    ACQ_SSB_CASE(32, 25, 8, 2) ACQ_SSB_CASE(32, 20, 8, 2) ACQ_SSB_CASE(32, 40, 4, 2) ACQ_SSB_CASE(20, 20, 8, 2)
+    ACQ_SSB_CASE(16, 25, 8, 1) ACQ_SSB_CASE(20, 10, 16, 2)
+    return nullptr;
+}
+
 SearchFn pick_search_warp(int mode, int ndop, int* pc) {
     if (mode == 2) {
         ACQ_SW_CASE(2, 40) ACQ_SW_CASE(2, 100) ACQ_SW_CASE(2, 120) ACQ_SW_CASE(2, 160) ACQ_SW_CASE(2, 200)

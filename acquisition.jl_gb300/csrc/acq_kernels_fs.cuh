@@ -778,6 +778,146 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
     }
 }
 
+// ------------------------------------------------------------------ data-bit / bit-edge search, split
+// Sign search (src/noncoherent_integration.jl:60-115) with the FFT split ndop = N1 x N2. For bit
+// edge e every data-bit pattern p transforms v_p = sum_b s(p, b) x_b, x_b the b-th sub-block of
+// the edge-shifted column zero-padded to ndop (src/sign_patterns.jl:23-47). By linearity pass 1
+// transforms each sub-block once (its inputs are zero for n1 >= N1 / NDB, known at compile time)
+// and pass 2 combines the sub-block results with each pattern's signs while loading. Pass-2
+// thread (p, k1, t) keeps the running max over the edges for its pattern in registers; the NP
+// patterns' maxima are merged at the end in candidate order (e, p) (strict '>', earlier wins).
+// Same result as k_col_sign_fs. Block: NP * N1 * W threads.
+template <int N1, int N2, int W, int NDB>
+__global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W)
+    k_col_sign_sb(const float2* __restrict__ T, int spc, const float2* __restrict__ twD, const float* __restrict__ pats,
+                  int n_coh, int n_be, int edge_step, const int* __restrict__ slots, const int* __restrict__ drift,
+                  int first, float* __restrict__ acc, uint16_t* __restrict__ win, int spc_eff) {
+    constexpr int ND = N1 * N2, NP = 1 << (NDB - 1), SUB = ND / NDB, NZ = N1 / NDB;
+    static_assert(N1 % NDB == 0, "sub-blocks must align with pass-1 rows");
+    extern __shared__ float2 sm[];
+    float2* tile = sm;
+    float2* wk = tile + ND * W;                 // NDB pass-1 results
+    float2* tws = wk + NDB * ND * W;
+    float* sgn = reinterpret_cast<float*>(tws + ND);   // s(p, b), NP x NDB
+    const int tid = threadIdx.x;
+    const int pi = blockIdx.y;
+    const int slot = slots[pi];
+    const int c0 = blockIdx.x * W;
+    const int wv = min(W, spc - c0);
+    const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
+    for (int w = tid; w < ND * W; w += blockDim.x) {
+        const int e = w / W, t = w - (w / W) * W;
+        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+    }
+    for (int i = tid; i < ND; i += blockDim.x) tws[i] = twD[i];
+    if (tid < NP * NDB) {
+        const int pp = tid / NDB, b = tid - (tid / NDB) * NDB;
+        sgn[tid] = pats[(static_cast<int64_t>(slot) * NP + pp) * n_coh + b * (n_coh / NDB)];
+    }
+    __syncthreads();
+    // pass-2 role
+    const int p2 = tid / (N1 * W), r2 = tid - (tid / (N1 * W)) * (N1 * W);
+    const int k1 = r2 / W, t2 = r2 - (r2 / W) * W;
+    float best[N2];
+    int bwin[N2];
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+        best[k2] = 0.f;
+        bwin[k2] = 0;
+    }
+    for (int e = 0; e < n_be; ++e) {
+        const int off = (e * edge_step) % ND;
+        for (int task = tid; task < NDB * N2 * W; task += blockDim.x) {
+            const int b = task / (N2 * W), r = task - (task / (N2 * W)) * (N2 * W);
+            const int n2 = r / W, t = r - (r / W) * W;
+            int base = off + b * SUB + n2;
+            base = base >= ND ? base - ND : base;
+            base = base >= ND ? base - ND : base;
+            float2 v[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; ++n1) {
+                if (n1 < NZ) {
+                    int row = base + N2 * n1;
+                    row = row >= ND ? row - ND : row;
+                    v[n1] = tile[row * W + t];
+                } else {
+                    v[n1] = make_float2(0.f, 0.f);
+                }
+            }
+            RegFFT<N1, false>::run(v);
+            float2* x = wk + b * ND * W;
+            static_for<0, N1>([&](auto kc) {
+                constexpr int kk = decltype(kc)::value;
+                constexpr int pr = reg_perm(N1, kk);
+                float2 y = v[pr];
+                if (kk != 0) y = c_mul(y, tws[n2 * kk]);
+                x[(n2 + N2 * kk) * W + t] = y;
+            });
+        }
+        __syncthreads();
+        {
+            float s[NDB];
+#pragma unroll
+            for (int b = 0; b < NDB; ++b) s[b] = sgn[p2 * NDB + b];
+            float2 v[N2];
+#pragma unroll
+            for (int m = 0; m < N2; ++m) {
+                float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int b = 0; b < NDB; ++b) {
+                    const float2 y = wk[b * ND * W + (N2 * k1 + m) * W + t2];
+                    a = b == 0 ? make_float2(s[0] * y.x, s[0] * y.y) : make_float2(a.x + s[b] * y.x, a.y + s[b] * y.y);
+                }
+                v[m] = a;
+            }
+            RegFFT<N2, false>::run(v);
+            const int cand = e * NP + p2;
+            static_for<0, N2>([&](auto kc) {
+                constexpr int k2 = decltype(kc)::value;
+                constexpr int pr = reg_perm(N2, k2);
+                const float2 x = v[pr];
+                const float pw = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+                const bool take = pw > best[k2];
+                best[k2] = take ? pw : best[k2];
+                bwin[k2] = take ? cand : bwin[k2];
+            });
+        }
+        __syncthreads();
+    }
+    // merge the patterns' maxima (candidate order (e, p)), stage, scatter
+    float* stg = reinterpret_cast<float*>(wk);
+    uint16_t* wst = reinterpret_cast<uint16_t*>(stg + NP * ND * W);
+    constexpr int half = ND / 2;
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+        const int om = k1 + N1 * k2;
+        const int row = om < half ? om + half : om - half;
+        stg[(p2 * ND + row) * W + t2] = best[k2];
+        wst[(p2 * ND + row) * W + t2] = static_cast<uint16_t>(bwin[k2]);
+    }
+    __syncthreads();
+    if (NP > 1) {
+        for (int w = tid; w < ND * W; w += blockDim.x) {
+            float bv = stg[w];
+            int bw = wst[w];
+            for (int q = 1; q < NP; ++q) {
+                const float v = stg[q * ND * W + w];
+                const int c = wst[q * ND * W + w];
+                if (v > bv || (v == bv && c < bw)) {
+                    bv = v;
+                    bw = c;
+                }
+            }
+            stg[w] = bv;
+            wst[w] = static_cast<uint16_t>(bw);
+        }
+        __syncthreads();
+    }
+    float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
+    uint16_t* wp = win + static_cast<int64_t>(pi) * ND * spc_eff;
+    scatter_rmw<W>(stg, wst, ND * W, tid, blockDim.x, wv, c0, spc, spc_eff, 0, drift, first, ap, wp);
+}
+
 // ------------------------------------------------------------------ warp-per-column search stage
 // Sign (MODE 1) or rotation (MODE 2) search with one warp per code-phase column: the CTA loads an
 // (ndop x 8) tile once, then every warp runs all candidates of its column with warp-level sync

@@ -162,6 +162,10 @@ struct acq_plan {
     int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1;
     std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
+    // data-bit / bit-edge stage split by sub-blocks
+    SignSbFn sign_sb = nullptr;
+    size_t smem_ssb = 0;
+    int Wssb = 8, threads_ssb = 256;
     // rotation stage split by sub-blocks
     RotSbFn rot_sb = nullptr;
     size_t smem_rsb = 0;
@@ -402,6 +406,18 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     if (!getenv_flag("ACQ_GENERIC_FFT") && (g.ndop % 2) == 0) {
         if (g.path == 1) P->sign_fs = pick_sign_fs(g.ndop);
         if (g.path == 2) P->rot_fs = pick_rot_fs(g.ndop);
+    }
+    if (g.path == 1 && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT") && (g.n_coh % g.ndb) == 0) {
+        int w = 8, th = 256;
+        size_t smem = 0;
+        SignSbFn fn = pick_sign_sb(g.ndop, g.ndb, &w, &th, &smem);
+        if (fn && smem <= 220 * 1024) {
+            set_smem((const void*)fn, smem);
+            P->sign_sb = fn;
+            P->smem_ssb = smem;
+            P->Wssb = w;
+            P->threads_ssb = th;
+        }
     }
     if (g.path == 2 && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT")) {
         int w = 8, th = 256;
@@ -686,6 +702,11 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             sp.use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0; sp.slots = a.d_slots; sp.drift = dr; sp.first = first;
             sp.acc = P->accb.as<float>(); sp.win = P->winb.as<uint16_t>();
             P->search_warp<<<dim3((g.spc + 7) / 8, n), kThreads, P->smem_search, st>>>(sp);
+        } else if (g.path == 1 && P->sign_sb) {
+            const int W = P->Wssb;
+            P->sign_sb<<<dim3((g.spc + W - 1) / W, n), P->threads_ssb, P->smem_ssb, st>>>(
+                P->T.as<float2>(), g.spc, P->fftD.tw, P->pats.as<float>(), g.n_coh, g.n_be, P->edge_step, a.d_slots,
+                dr, first | (last ? 2 : 0), P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 1 && P->sign_fs) {
             const int W = P->Wsfs;
             P->sign_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
