@@ -24,6 +24,7 @@ ACQ_CF32, ACQ_CI16, ACQ_CI8, ACQ_CF64 = 0, 1, 2, 3
 ACQ_NOISE_OPPOSITE_ROW, ACQ_NOISE_GLOBAL_MEAN = 0, 1
 ACQ_FLAG_SUBSAMPLE_INTERP = 1
 ACQ_FLAG_STORE_POWER_BINS = 2
+ACQ_FLAG_POWER_BINS_CHIP_SORTED = 4
 
 
 class PlanDesc(C.Structure):
@@ -77,7 +78,7 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_batch_create", "acq_batch_destroy", "acq_batch_input_ptr", "acq_batch_upload", "acq_batch_launch",
             "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
             "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine",
-            "acq_plan_get_option"]
+            "acq_plan_get_option", "acq_chip_order", "acq_sort_power_bins_by_chip"]
 ACQ_OPT_FORM = 0
 ACQ_OPT_ROTATION_PRECISION = 1
 ACQ_OPT_MMA_SCALE_LOG2 = 2
@@ -126,6 +127,9 @@ def load():
                                                        C.c_int32, C.c_void_p, C.c_void_p]
     lib.acq_plan_set_option.argtypes = [P, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
     lib.acq_plan_get_option.argtypes = [P, C.c_int32, C.POINTER(C.c_int64)]
+    lib.acq_chip_order.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.c_double, C.c_double, C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_double)]
+    lib.acq_sort_power_bins_by_chip.argtypes = [P, P, C.c_int32, P, P]
     lib.acq_corr_create.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int8),
                                     C.POINTER(P)]
     lib.acq_corr_destroy.argtypes = [P]

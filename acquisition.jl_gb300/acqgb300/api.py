@@ -344,17 +344,39 @@ def _results(plan: AcquisitionPlan, res_arr, prns, store_power_bins, bins):
     return out
 
 
-def _flags(subsample_interpolation, store_power_bins):
+def _flags(subsample_interpolation, store_power_bins, chip_sorted=False):
     return ((L.ACQ_FLAG_SUBSAMPLE_INTERP if subsample_interpolation else 0)
-            | (L.ACQ_FLAG_STORE_POWER_BINS if store_power_bins else 0))
+            | (L.ACQ_FLAG_STORE_POWER_BINS if store_power_bins else 0)
+            | (L.ACQ_FLAG_POWER_BINS_CHIP_SORTED if (store_power_bins and chip_sorted) else 0))
+
+
+def chip_order(num_blocks: int, block_size: int, width: int, code_freq: float, sampling_freq: float):
+    """(perm, chip_axis): the FM-DBZP column shown at each chip-sorted position and its code phase
+    in chips (src/plot.jl:16-20,35-57, ``_fmdbzp_sort_by_chip``)."""
+    perm = np.empty(int(width), np.int32)
+    axis = np.empty(int(width), np.float64)
+    _check(L.load().acq_chip_order(int(num_blocks), int(block_size), int(width), float(code_freq),
+                                   float(sampling_freq), perm.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   axis.ctypes.data_as(C.POINTER(C.c_double))))
+    return perm, axis
+
+
+def plan_chip_axis(plan: "AcquisitionPlan") -> np.ndarray:
+    """Code phase (chips) of every column of a chip-sorted power surface of this plan."""
+    g = plan.geometry
+    return chip_order(g.num_blocks, g.block_size, g.samples_per_code_eff, plan.system.code_frequency,
+                      plan.sampling_freq)[1]
 
 
 def acquire_b(plan: AcquisitionPlan, signal, prns, *, interm_freq: float = 0.0,
-              subsample_interpolation: bool = False, store_power_bins: bool = False):
+              subsample_interpolation: bool = False, store_power_bins: bool = False,
+              chip_sorted_power_bins: bool = False):
     """``acquire!(plan, signal, prns; interm_freq, subsample_interpolation, store_power_bins)``.
 
     ``signal`` is a host array (complex64/complex128, or (..., 2) int16/int8 interleaved) or a
     CUDA tensor (see :func:`acquire_device`). A scalar ``prns`` returns one result.
+    ``chip_sorted_power_bins`` returns the surfaces with columns in code-phase order
+    (:func:`plan_chip_axis` gives the axis) instead of FM-DBZP order.
     """
     single = np.ndim(prns) == 0
     prn_list = [int(p) for p in np.atleast_1d(prns)]
@@ -373,7 +395,8 @@ def acquire_b(plan: AcquisitionPlan, signal, prns, *, interm_freq: float = 0.0,
         bins_ptr = bins.ctypes.data_as(C.POINTER(C.c_float))
     prn_arr = (C.c_int32 * len(prn_list))(*prn_list)
     _check(lib.acq_acquire(plan.handle, arr.ctypes.data_as(C.c_void_p), dt, int(n), prn_arr, len(prn_list),
-                           float(interm_freq), _flags(subsample_interpolation, store_power_bins), res, bins_ptr))
+                           float(interm_freq), _flags(subsample_interpolation, store_power_bins,
+                                                      chip_sorted_power_bins), res, bins_ptr))
     out = _results(plan, res, prn_list, store_power_bins, bins)
     return out[0] if single else out
 

@@ -424,4 +424,31 @@ double cfar_threshold(double pfa, int64_t num_cells, int M) {
     return x / a;
 }
 
+// src/plot.jl:16-20 (_fmdbzp_column_to_tau) and :35-57 (_fmdbzp_sort_by_chip): chip phase
+// mod(-tau * fc / fs, code_length) per column with Julia's floating-point mod, then a stable
+// sort (Julia's sortperm keeps equal keys in index order).
+void chip_order(int num_blocks, int block_size, int64_t width, double code_freq, double fs, int32_t* perm,
+                double* axis) {
+    if (num_blocks < 1 || block_size < 1 || width < 1 || !(code_freq > 0) || !(fs > 0))
+        throw AcqError(ACQ_ERR_ARGUMENT, "chip order needs positive num_blocks, block_size, width and frequencies");
+    const double code_length = static_cast<double>(width) * code_freq / fs;
+    std::vector<double> chip(static_cast<size_t>(width));
+    for (int64_t c = 0; c < width; ++c) {
+        const int64_t block_row = c / block_size, within = c % block_size;
+        const int64_t tau = (((num_blocks - block_row) % num_blocks + num_blocks) % num_blocks) * block_size + within;
+        const double x = -static_cast<double>(tau) * code_freq / fs;
+        double r = std::fmod(x, code_length);
+        if (r == 0.0) r = 0.0;                  // copysign(r, code_length)
+        else if ((r > 0) != (code_length > 0)) r += code_length;
+        chip[static_cast<size_t>(c)] = r;
+    }
+    std::vector<int32_t> idx(static_cast<size_t>(width));
+    for (int64_t i = 0; i < width; ++i) idx[static_cast<size_t>(i)] = static_cast<int32_t>(i);
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return chip[a] < chip[b]; });
+    for (int64_t i = 0; i < width; ++i) {
+        perm[i] = idx[static_cast<size_t>(i)];
+        if (axis) axis[i] = chip[static_cast<size_t>(idx[static_cast<size_t>(i)])];
+    }
+}
+
 }  // namespace acq

@@ -61,6 +61,11 @@ bool code_drift_shifts(const Geometry& g, const SystemInfo& s, double fs, int st
 
 double cfar_threshold(double pfa, int64_t num_cells, int M);   // src/cfar.jl:64-85
 
+// Column order of a power surface sorted by code phase (src/plot.jl:16-20,35-57): perm[i] is the
+// FM-DBZP column shown at position i, axis[i] its code phase in chips (monotone).
+void chip_order(int num_blocks, int block_size, int64_t width, double code_freq, double fs, int32_t* perm,
+                double* axis);
+
 int nextprod_2357(int n);
 
 // Record the calling thread's last error message (read back by acq_last_error).

@@ -39,6 +39,17 @@ struct CudaError : AcqError {
 constexpr int kThreads = 256;
 constexpr size_t kSmemBudget = 200 * 1024;   // dynamic shared memory per CTA we plan for
 
+// out[r][i] = in[r][perm[i]] for rows of `width` columns (chip-sorted power surfaces)
+__global__ void k_gather_cols(const float* __restrict__ in, int64_t rows, int64_t width, const int32_t* __restrict__ perm,
+                              float* __restrict__ out) {
+    const int64_t total = rows * width;
+    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = k / width, i = k - r * width;
+        out[k] = in[r * width + perm[i]];
+    }
+}
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -188,6 +199,7 @@ struct acq_plan {
     ColTmaFn col_tma = nullptr;
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
+    DevBuf chipperm, sorted;   // chip-sorted surface export (src/plot.jl:35-57)
     int tmaW = 16, tmaBoxRows = 1, tmaBoxes = 1, tmaGrid = 1, tmaH = 0, tmaCtasPerSm = 0;
     int n_plan_prns = 0;
     size_t smem_col_tma = 0;
@@ -466,6 +478,12 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     setup_fused(P);
     P->n_plan_prns = n_prns;
     setup_col_tma(P, n_prns);
+    {
+        std::vector<int32_t> perm(g.spc_eff);
+        chip_order(g.nb, g.bs, g.spc_eff, P->sys->code_freq, P->desc.sampling_freq_hz, perm.data(), nullptr);
+        P->chipperm.ensure(sizeof(int32_t) * perm.size());
+        CK(cudaMemcpy(P->chipperm.p, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice));
+    }
 
     // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
     std::vector<int8_t> h_codes(static_cast<size_t>(n_prns) * g.spc);
@@ -940,9 +958,19 @@ void fetch(acq_plan* P, acq_result* results, float* power_bins) {
     CK(cudaSetDevice(P->device));
     if (results)
         CK(cudaMemcpyAsync(results, P->res.p, sizeof(acq_result) * P->last_n, cudaMemcpyDeviceToHost, P->stream));
-    if (power_bins && (P->last_flags & ACQ_FLAG_STORE_POWER_BINS))
-        CK(cudaMemcpyAsync(power_bins, P->accb.p, sizeof(float) * (size_t)P->last_n * g.ndop * g.spc_eff,
-                           cudaMemcpyDeviceToHost, P->stream));
+    if (power_bins && (P->last_flags & ACQ_FLAG_STORE_POWER_BINS)) {
+        const size_t cells = (size_t)P->last_n * g.ndop * g.spc_eff;
+        const void* src = P->accb.p;
+        if (P->last_flags & ACQ_FLAG_POWER_BINS_CHIP_SORTED) {
+            P->sorted.ensure(sizeof(float) * cells);
+            const int64_t rows = (int64_t)P->last_n * g.ndop;
+            k_gather_cols<<<std::min<int64_t>((rows * g.spc_eff + 255) / 256, 8192), 256, 0, P->stream>>>(
+                P->accb.as<float>(), rows, g.spc_eff, P->chipperm.as<int32_t>(), P->sorted.as<float>());
+            CK(cudaGetLastError());
+            src = P->sorted.p;
+        }
+        CK(cudaMemcpyAsync(power_bins, src, sizeof(float) * cells, cudaMemcpyDeviceToHost, P->stream));
+    }
     CK(cudaStreamSynchronize(P->stream));
     t_collect(P);
     if (P->errflag.p) {
@@ -1056,7 +1084,7 @@ int acq_plan_destroy(acq_plan* P) {
     if (P->stream) cudaStreamSynchronize(P->stream);
     for (DevBuf* b : {&P->twF, &P->twD, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
                       &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
-                      &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag})
+                      &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted})
         b->reset();
     for (cudaEvent_t e : P->ev_start) cudaEventDestroy(e);
     for (cudaEvent_t e : P->ev_stop) cudaEventDestroy(e);
@@ -1349,6 +1377,30 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t M, double* out) {
     return guarded([&] {
         if (!out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         *out = cfar_threshold(pfa, num_cells, M);
+    });
+}
+
+int acq_chip_order(int32_t num_blocks, int32_t block_size, int64_t width, double code_freq_hz, double sampling_freq_hz,
+                   int32_t* perm, double* chip_axis) {
+    return guarded([&] {
+        if (!perm) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        chip_order(num_blocks, block_size, width, code_freq_hz, sampling_freq_hz, perm, chip_axis);
+    });
+}
+
+int acq_sort_power_bins_by_chip(const acq_plan* P, const float* d_power_bins, int32_t n_surfaces, float* d_out,
+                                void* stream) {
+    return guarded([&] {
+        if (!P || !d_power_bins || !d_out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (n_surfaces < 1) throw AcqError(ACQ_ERR_ARGUMENT, "n_surfaces must be >= 1");
+        if (d_power_bins == d_out) throw AcqError(ACQ_ERR_ARGUMENT, "the sort cannot run in place");
+        const Geometry& g = P->g;
+        CK(cudaSetDevice(P->device));
+        const int64_t rows = (int64_t)n_surfaces * g.ndop;
+        k_gather_cols<<<std::min<int64_t>((rows * g.spc_eff + 255) / 256, 8192), 256, 0,
+                        static_cast<cudaStream_t>(stream)>>>(d_power_bins, rows, g.spc_eff,
+                                                             P->chipperm.as<int32_t>(), d_out);
+        CK(cudaGetLastError());
     });
 }
 

@@ -50,6 +50,8 @@ extern "C" {
 
 #define ACQ_FLAG_SUBSAMPLE_INTERP 1u /* acquire!(...; subsample_interpolation = true) */
 #define ACQ_FLAG_STORE_POWER_BINS 2u /* acquire!(...; store_power_bins = true) */
+#define ACQ_FLAG_POWER_BINS_CHIP_SORTED 4u /* with STORE_POWER_BINS: columns in code-phase order
+                                              (src/plot.jl:35-57) instead of FM-DBZP order */
 
 typedef struct acq_plan acq_plan;
 
@@ -253,6 +255,17 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_in
 
 /* gen_code(n, system, prn, sampling_freq, code_freq, start_phase) into `out` (+-1 int8).
  * code_freq_hz <= 0 selects the system's nominal code rate. Host only. */
+/* Column order of a power surface sorted by code phase, src/plot.jl:16-20,35-57 (host, no GPU):
+ * perm[i] = the FM-DBZP column at chip-sorted position i (width entries), chip_axis[i] (may be
+ * NULL) its code phase in chips, monotone. width = the surface's columns (samples_per_code_eff). */
+int acq_chip_order(int32_t num_blocks, int32_t block_size, int64_t width, double code_freq_hz, double sampling_freq_hz,
+                   int32_t* perm, double* chip_axis);
+
+/* Chip-sorted copy of n_surfaces device surfaces (num_doppler_bins x samples_per_code_eff each,
+ * the layout acquisitions store) into d_out (device; not in place), enqueued on `stream`. */
+int acq_sort_power_bins_by_chip(const acq_plan* plan, const float* d_power_bins, int32_t n_surfaces, float* d_out,
+                                void* stream);
+
 int acq_gen_code(int32_t system, int32_t prn, int64_t n, double sampling_freq_hz, double code_freq_hz,
                  double start_phase, int8_t* out);
 

@@ -715,6 +715,32 @@ def acquire_b(plan: Plan, signal, prns, *, interm_freq: float = 0.0, subsample_i
 
 
 # --------------------------------------------------------------------------------------
+# chip-sorted surface, src/plot.jl:16-20,35-57
+# --------------------------------------------------------------------------------------
+def fmdbzp_column_to_tau(c: int, num_blocks: int, block_size: int) -> int:
+    """src/plot.jl:16-20."""
+    return ((num_blocks - c // block_size) % num_blocks) * block_size + c % block_size
+
+
+def _julia_fmod(x: float, y: float) -> float:
+    r = math.fmod(x, y)
+    if r == 0.0:
+        return math.copysign(0.0, y)
+    return r + y if (r > 0) != (y > 0) else r
+
+
+def fmdbzp_sort_by_chip(power_bins: np.ndarray, num_blocks: int, block_size: int, code_freq: float,
+                        fs: float):
+    """src/plot.jl:35-57 -> (chip_axis, chip_sorted_power_bins, chip_order)."""
+    width = power_bins.shape[1]
+    code_length = width * code_freq / fs
+    chip = np.array([_julia_fmod(-fmdbzp_column_to_tau(c, num_blocks, block_size) * code_freq / fs, code_length)
+                     for c in range(width)])
+    order = np.argsort(chip, kind="stable")
+    return chip[order], power_bins[:, order], order
+
+
+# --------------------------------------------------------------------------------------
 # signal model, src/generate_test_signal.jl:45-68 (code Doppler, carrier, AWGN)
 # --------------------------------------------------------------------------------------
 def clean_signal(system: System, prn: int, n: int, fs: float, doppler: float, code_phase: float,

@@ -159,3 +159,24 @@ def test_correlator_create_fails_loudly_without_gpu():
     bad = (C.c_int32 * 1)(40)
     assert lib.acq_corr_create(L.ACQ_GPS_L1CA, 10e6, bad, 1, None, C.byref(h)) == L.ACQ_ERR_ARGUMENT
     assert "PRN must be in 1:32" in L.last_error()
+
+
+@pytest.mark.parametrize("nb,bs,width,fs", [(4, 8, 32, 1.023e6 * 32 / 1023), (16, 128, 2048, 2.048e6),
+                                             (20, 250, 5000, 5e6), (25, 800, 200000, 20e6), (16, 250, 4000, 4e6)])
+def test_chip_order_matches_oracle(nb, bs, width, fs):
+    perm, axis = A.chip_order(nb, bs, width, 1.023e6, fs)
+    dummy = np.arange(width, dtype=np.float32)[None, :]
+    o_axis, o_sorted, o_order = O.fmdbzp_sort_by_chip(dummy, nb, bs, 1.023e6, fs)
+    assert np.array_equal(perm, o_order)
+    assert np.array_equal(axis, o_axis)
+    # test/plot.jl:56-76 properties: monotone, within [0, code_length), unique
+    assert np.all(np.diff(axis) >= 0) and axis.min() >= 0 and axis.max() < width * 1.023e6 / fs
+    if width == nb * bs:      # one code period: a bijection (rotation surfaces repeat every period)
+        assert len(np.unique(axis)) == width
+
+
+def test_column_to_tau_known_answers():
+    # test/plot.jl:18-41
+    assert [O.fmdbzp_column_to_tau(c, 4, 8) for c in (0, 1, 8, 16, 24)] == [0, 1, 24, 16, 8]
+    assert O.fmdbzp_column_to_tau(0, 32, 64) == 0
+    assert sorted(O.fmdbzp_column_to_tau(c, 4, 8) for c in range(32)) == list(range(32))
