@@ -427,6 +427,8 @@ double cfar_threshold(double pfa, int64_t num_cells, int M) {
 // src/plot.jl:16-20 (_fmdbzp_column_to_tau) and :35-57 (_fmdbzp_sort_by_chip): chip phase
 // mod(-tau * fc / fs, code_length) per column with Julia's floating-point mod, then a stable
 // sort (Julia's sortperm keeps equal keys in index order).
+bool is_whole_freq(double x) { return is_whole(x); }
+
 void chip_order(int num_blocks, int block_size, int64_t width, double code_freq, double fs, int32_t* perm,
                 double* axis) {
     if (num_blocks < 1 || block_size < 1 || width < 1 || !(code_freq > 0) || !(fs > 0))

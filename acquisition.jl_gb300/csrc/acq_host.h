@@ -49,6 +49,9 @@ Geometry compute_geometry(const acq_plan_desc& d);   // throws AcqError(ACQ_ERR_
 // +-1 chips of the full (primary x secondary) code of a PRN.
 std::vector<int8_t> full_chips(int system, int prn);
 
+// true when x is an integer representable exactly (gen_code's exact integer phase path)
+bool is_whole_freq(double x);
+
 // GNSSSignals gen_code semantics (sample i -> chip floor(start + i*fc/fs) mod full length).
 void gen_code(int system, int prn, int64_t n, double fs, double fc, double start_phase, int8_t* out);
 

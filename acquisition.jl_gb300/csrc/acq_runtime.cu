@@ -39,6 +39,50 @@ struct CudaError : AcqError {
 constexpr int kThreads = 256;
 constexpr size_t kSmemBudget = 200 * 1024;   // dynamic shared memory per CTA we plan for
 
+// Sampled codes on the device with GNSSSignals gen_code semantics (the host restatement is
+// acq::gen_code): sample i of PRN p takes chip floor(sp + i fc / fs) mod L of that PRN's table,
+// negated in the second half of the chip for BOC(1,1). Whole fs and fc with sp = 0 use exact
+// integer arithmetic; otherwise the FP64 phase is formed with explicit round-to-nearest
+// multiply and add (no contraction), as on the host.
+__global__ void k_sample_codes(const int8_t* __restrict__ chips, int64_t L, int n_prns, int64_t n, int64_t fci,
+                               int64_t fsi, int whole, double sp, double ratio, int boc, int8_t* __restrict__ out) {
+    const int64_t total = static_cast<int64_t>(n_prns) * n;
+    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t p = k / n, i = k - p * n;
+        int64_t idx;
+        bool second;
+        if (whole) {
+            const int64_t num = i * fci;
+            idx = num / fsi;
+            second = 2 * (num - idx * fsi) >= fsi;
+        } else {
+            const double ph = __dadd_rn(sp, __dmul_rn(static_cast<double>(i), ratio));
+            const double fl = floor(ph);
+            idx = static_cast<int64_t>(fl);
+            second = __dsub_rn(ph, fl) >= 0.5;
+        }
+        int8_t v = chips[p * L + ((idx % L) + L) % L];
+        if (boc && second) v = static_cast<int8_t>(-v);
+        out[k] = v;
+    }
+}
+
+void sample_codes_device(int system, const int8_t* d_chips, int64_t L, int n_prns, int64_t n, double fs, double fc,
+                         double start, int8_t* d_out, cudaStream_t st) {
+    const SystemInfo& s = system_info(system);
+    if (fc <= 0) fc = s.code_freq;
+    double sp = std::fmod(start, static_cast<double>(L));
+    if (sp < 0) sp += L;
+    const int whole = (sp == 0.0 && is_whole_freq(fs) && is_whole_freq(fc)) ? 1 : 0;
+    const int64_t total = static_cast<int64_t>(n_prns) * n;
+    if (total <= 0) return;
+    k_sample_codes<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 16384)), 256, 0, st>>>(
+        d_chips, L, n_prns, n, whole ? static_cast<int64_t>(fc) : 0, whole ? static_cast<int64_t>(fs) : 1, whole, sp,
+        fc / fs, s.boc11 ? 1 : 0, d_out);
+    CK(cudaGetLastError());
+}
+
 // out[r][i] = in[r][perm[i]] for rows of `width` columns (chip-sorted power surfaces)
 __global__ void k_gather_cols(const float* __restrict__ in, int64_t rows, int64_t width, const int32_t* __restrict__ perm,
                               float* __restrict__ out) {
@@ -485,31 +529,33 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         CK(cudaMemcpy(P->chipperm.p, perm.data(), sizeof(int32_t) * perm.size(), cudaMemcpyHostToDevice));
     }
 
-    // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251
-    std::vector<int8_t> h_codes(static_cast<size_t>(n_prns) * g.spc);
-    for (int i = 0; i < n_prns; ++i) {
-        if (user_codes)
-            std::memcpy(&h_codes[(size_t)i * g.spc], user_codes + (size_t)i * g.spc, g.spc);
-        else
-            gen_code(P->desc.system, prns[i], g.spc, P->desc.sampling_freq_hz, 0.0, 0.0, &h_codes[(size_t)i * g.spc]);
-    }
-    P->codes.ensure(h_codes.size());
-    CK(cudaMemcpy(P->codes.p, h_codes.data(), h_codes.size(), cudaMemcpyHostToDevice));
-    P->conj.ensure(sizeof(float2) * (size_t)n_prns * g.nb * g.fft_size);
-    k_code_spectra<<<n_prns * g.nb, kThreads, P->smem_front, P->stream>>>(P->codes.as<int8_t>(), g.spc, g.nb, g.bs,
-                                                                           P->fftF, P->conj.as<float2>());
-    CK(cudaGetLastError());
-    // full chip tables for the secondary-code despread (rotation path only)
-    if (g.path == 2) {
+    // codes (GNSSSignals gen_code semantics) and conj code-block spectra, src/plan.jl:230-251:
+    // chip tables (LFSR / memory codes, secondary folded in) built on the host, sampled on the
+    // device; user codes are uploaded as given
+    {
         std::vector<int8_t> c0 = full_chips(P->desc.system, prns[0]);
         P->chips_len = static_cast<int64_t>(c0.size());
         std::vector<int8_t> all((size_t)n_prns * P->chips_len);
         for (int i = 0; i < n_prns; ++i) {
-            std::vector<int8_t> c = full_chips(P->desc.system, prns[i]);
+            std::vector<int8_t> c = i == 0 ? c0 : full_chips(P->desc.system, prns[i]);
             std::memcpy(&all[(size_t)i * P->chips_len], c.data(), P->chips_len);
         }
         P->chips.ensure(all.size());
         CK(cudaMemcpy(P->chips.p, all.data(), all.size(), cudaMemcpyHostToDevice));
+    }
+    P->codes.ensure((size_t)n_prns * g.spc);
+    if (user_codes) {
+        CK(cudaMemcpy(P->codes.p, user_codes, (size_t)n_prns * g.spc, cudaMemcpyHostToDevice));
+    } else {
+        sample_codes_device(P->desc.system, P->chips.as<int8_t>(), P->chips_len, n_prns, g.spc,
+                            P->desc.sampling_freq_hz, 0.0, 0.0, P->codes.as<int8_t>(), P->stream);
+    }
+    P->conj.ensure(sizeof(float2) * (size_t)n_prns * g.nb * g.fft_size);
+    k_code_spectra<<<n_prns * g.nb, kThreads, P->smem_front, P->stream>>>(P->codes.as<int8_t>(), g.spc, g.nb, g.bs,
+                                                                           P->fftF, P->conj.as<float2>());
+    CK(cudaGetLastError());
+    // secondary code for the secondary-code despread (rotation path only)
+    if (g.path == 2) {
         P->sec.ensure(P->sys->secondary_length);
         CK(cudaMemcpy(P->sec.p, P->sys->secondary, P->sys->secondary_length, cudaMemcpyHostToDevice));
     }
@@ -1377,6 +1423,29 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t M, double* out) {
     return guarded([&] {
         if (!out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         *out = cfar_threshold(pfa, num_cells, M);
+    });
+}
+
+int acq_gen_code_device(int32_t system, const int32_t* prns, int32_t n_prns, int64_t n, double fs, double fc,
+                        double start_phase, int8_t* d_out, void* stream) {
+    return guarded([&] {
+        if (!prns || !d_out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (n_prns < 1 || n < 0) throw AcqError(ACQ_ERR_ARGUMENT, "n_prns must be >= 1 and n >= 0");
+        if (!(fs > 0)) throw AcqError(ACQ_ERR_ARGUMENT, "sampling frequency must be positive");
+        std::vector<int8_t> c0 = full_chips(system, prns[0]);
+        const int64_t L = static_cast<int64_t>(c0.size());
+        std::vector<int8_t> all((size_t)n_prns * L);
+        for (int i = 0; i < n_prns; ++i) {
+            std::vector<int8_t> c = full_chips(system, prns[i]);
+            std::memcpy(&all[(size_t)i * L], c.data(), L);
+        }
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        int8_t* d_chips = nullptr;
+        CK(cudaMallocAsync(reinterpret_cast<void**>(&d_chips), all.size(), st));
+        CK(cudaMemcpyAsync(d_chips, all.data(), all.size(), cudaMemcpyHostToDevice, st));
+        sample_codes_device(system, d_chips, L, n_prns, n, fs, fc, start_phase, d_out, st);
+        CK(cudaFreeAsync(d_chips, st));
+        CK(cudaStreamSynchronize(st));   // the host chip tables go out of scope
     });
 }
 

@@ -578,10 +578,21 @@ def main():
     ap.add_argument("--no-precision-study", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default launch shapes (otherwise the autotuner picks them before timing)")
+    ap.add_argument("--prns", type=int, default=None,
+                    help="search PRNs 1..N instead of 1..32 (profiling cases only; the workload name says so)")
+    ap.add_argument("--cells-per-prn", type=int, default=None,
+                    help="fine search: cells per PRN (profiling cases only; default 1024)")
     ap.add_argument("--accumulations", type=int, default=None,
                     help="non-coherent accumulations (profiling cases only; default: the workload's)")
     args = ap.parse_args()
     set_config(args.config)
+    global PRNS, WORKLOAD
+    if args.prns:
+        PRNS = list(range(1, int(args.prns) + 1))
+        WORKLOAD = f"{WORKLOAD}_{len(PRNS)}prn"
+    if args.cells_per_prn:
+        CFG["cells_per_prn"] = int(args.cells_per_prn)
+        WORKLOAD = f"{WORKLOAD}_{int(args.cells_per_prn)}cells"
     args.warmup = max(args.warmup, 3)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

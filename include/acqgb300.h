@@ -255,6 +255,12 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_in
 
 /* gen_code(n, system, prn, sampling_freq, code_freq, start_phase) into `out` (+-1 int8).
  * code_freq_hz <= 0 selects the system's nominal code rate. Host only. */
+/* gen_code on the device for n_prns PRNs: d_out (device, n_prns x n int8) receives, per PRN,
+ * exactly what acq_gen_code returns for (system, prn, n, fs, fc, start_phase). Waits for
+ * `stream` before returning. */
+int acq_gen_code_device(int32_t system, const int32_t* prns, int32_t n_prns, int64_t n, double sampling_freq_hz,
+                        double code_freq_hz, double start_phase, int8_t* d_out, void* stream);
+
 /* Column order of a power surface sorted by code phase, src/plot.jl:16-20,35-57 (host, no GPU):
  * perm[i] = the FM-DBZP column at chip-sorted position i (width entries), chip_axis[i] (may be
  * NULL) its code phase in chips, monotone. width = the surface's columns (samples_per_code_eff). */
