@@ -261,6 +261,15 @@ class AcquisitionPlan:
         _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_ROTATION_PRECISION, val, C.byref(eff)))
         return {v: k for k, v in PRECISIONS.items()}[eff.value]
 
+    def set_doppler_precision(self, precision: str) -> str:
+        """Simple path: the per-column Doppler DFT as a dense DFT-matrix GEMM on the tensor cores
+        ('fp16', 'bf16', 'fp16_split', 'bf16_split'; ndop <= 250) or FP32 FFTs ('fp32', the
+        default). Returns the precision in effect."""
+        val = PRECISIONS[precision]
+        eff = C.c_int64()
+        _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_DOPPLER_PRECISION, val, C.byref(eff)))
+        return {v: k for k, v in PRECISIONS.items()}[eff.value]
+
     def set_mma_scale_log2(self, e: int | None):
         """Power-of-two scale of the spectra before FP16 rounding (None: by input type)."""
         _check(L.load().acq_plan_set_option(self._h, L.ACQ_OPT_MMA_SCALE_LOG2, 127 if e is None else int(e), None))

@@ -37,6 +37,8 @@ using SignSbFn = void (*)(const float2*, int, const float2*, const float*, int, 
 SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem);
 
 struct RotMmaParams;
+struct DftMmaParams;
+using DftMmaFn = void (*)(DftMmaParams);
 using RotMmaFn = void (*)(RotMmaParams);
 // tensor-core rotation combine for (coherent periods, blocks per period, candidates) at an
 // ACQ_PREC_* precision other than FP32; nullptr when not instantiated; *smem = dynamic bytes.

@@ -334,3 +334,217 @@ __global__ void __launch_bounds__(256, 2) k_rot_mma(RotMmaParams p) {
 }
 
 }  // namespace acq
+
+namespace acq {
+
+// ------------------------------------------------------------------ Doppler DFT as a GEMM
+// Simple-path column stage (src/acquire.jl:335-385, src/noncoherent_integration.jl:482-592)
+// with the ndop-point Doppler DFT of every code column as one dense complex DFT-matrix GEMM on
+// the tensor cores: for a block of 128 code columns,
+//   D[m = column, n = (k, re|im)] = sum_{kk = (g, re|im)} A[m, kk] B[n, kk],
+// A = the coherent tile (FP16/BF16, one operand or hi + lo), B = the real form of
+// exp(-2 pi i g k / ndop) (hi + lo in the split variants: A_hi B_hi + A_hi B_lo + A_lo B_hi, FP32
+// accumulation in TMEM). The K dimension streams through shared memory in steps of 8 rows
+// (16 real K): the block converts its tile rows while the tensor core works on the previous
+// step (two buffers, one mbarrier each); the DFT-matrix chunks come from global memory by
+// 16-byte cp.async. Epilogue: |X|^2, fftshift, destination-row drift, accumulation (loads of a
+// batch before its stores). ndop <= 256 (TMEM: 2 ndop <= 512 FP32 columns).
+constexpr int kDftCols = 128;       // code columns per block (MMA M)
+constexpr int kDftThreads = 256;
+
+struct DftMmaParams {
+    const float2* T;                // (n, ndop, spc) coherent tile of one step
+    int spc, nd, spc_eff, n_pad, ksteps, first, has_drift;
+    const int* drift;               // (ndop) destination-row shifts
+    float* acc;
+    const uint8_t* B;               // [split][ksteps][n_pad x 16] canonical K-major chunks
+    float scale;                    // power of two applied to the tile before rounding
+    int* err;
+};
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_all() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_zero() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int FMT, int NSPLIT>
+__global__ void __launch_bounds__(kDftThreads, 1) k_col_dft_mma(DftMmaParams p) {
+    constexpr int A_BYTES = kDftCols * 32;   // 128 rows x 16 K x 2 B
+    extern __shared__ uint8_t smraw_[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smraw_) + 1023) & ~uintptr_t(1023));
+    const int b_bytes = p.n_pad * 32;
+    uint8_t* Abuf = sm;                                        // [2][NSPLIT][A_BYTES]
+    uint8_t* Bbuf = sm + 2 * NSPLIT * A_BYTES;                 // [2][NSPLIT][b_bytes]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bbuf + 2 * NSPLIT * b_bytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int pi = blockIdx.y;
+    const int c0 = blockIdx.x * kDftCols;
+    const int nt0 = p.n_pad < 256 ? p.n_pad : 256, nt1 = p.n_pad - nt0;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    if (warp == 0) tc_alloc(tslot, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const float2* tp = p.T + static_cast<int64_t>(pi) * p.nd * p.spc;
+    // producer role: column m = tid % 128, rows g = 8 ks + 4 (tid / 128) .. + 3
+    const int m = tid & 127, half_rows = tid >> 7;
+    const int c = c0 + m;
+    uint32_t use[2] = {0, 0};
+    bool ok = true;
+    for (int ks = 0; ks < p.ksteps && ok; ++ks) {
+        const int b = ks & 1;
+        if (ks >= 2) {   // the MMAs of step ks-2 read this buffer
+            const bool mine = mbar_wait_bounded(&bar[b], (use[b] - 1) & 1, p.err, 5);
+            ok = __syncthreads_or(mine ? 0 : 1) == 0;
+            if (!ok) break;
+        }
+        // B chunks (constant DFT matrix) by 16-byte asynchronous copies
+        for (int s = 0; s < NSPLIT; ++s) {
+            const uint8_t* src = p.B + (static_cast<int64_t>(s) * p.ksteps + ks) * b_bytes;
+            uint8_t* dst = Bbuf + (b * NSPLIT + s) * b_bytes;
+            for (int o = tid * 16; o < b_bytes; o += kDftThreads * 16) cp_async16(dst + o, src + o);
+        }
+        cp_async_commit_all();
+        // A chunk: rows g = 8 ks + 4 half_rows + r of column c, K index 2 (g - 8 ks) + re|im
+        float2 v[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int g = 8 * ks + 4 * half_rows + r;
+            v[r] = (g < p.nd && c < p.spc) ? tp[static_cast<int64_t>(g) * p.spc + c] : make_float2(0.f, 0.f);
+            v[r].x *= p.scale;
+            v[r].y *= p.scale;
+        }
+        // the 8 K values of this thread are one 16-byte core-matrix row: chunk kc = half_rows
+        const int aoff = (m >> 3) * 256 + half_rows * 128 + (m & 7) * 16;
+        uint4 hi, lo;
+        uint32_t* hp = reinterpret_cast<uint32_t*>(&hi);
+        uint32_t* lp = reinterpret_cast<uint32_t*>(&lo);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            hp[r] = pack2<FMT>(v[r].x, v[r].y);
+            if (NSPLIT == 2) {
+                const float2 h = unpack2<FMT>(hp[r]);
+                lp[r] = pack2<FMT>(v[r].x - h.x, v[r].y - h.y);
+            }
+        }
+        *reinterpret_cast<uint4*>(Abuf + (b * NSPLIT + 0) * A_BYTES + aoff) = hi;
+        if (NSPLIT == 2) *reinterpret_cast<uint4*>(Abuf + (b * NSPLIT + 1) * A_BYTES + aoff) = lo;
+        cp_async_wait_zero();
+        fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            // products: hi*hi (+ hi*lo + lo*hi for the split variants)
+            const int np = NSPLIT == 2 ? 3 : 1;
+            for (int q = 0; q < np; ++q) {
+                const int sa = q == 2 ? 1 : 0, sb = q == 1 ? 1 : 0;
+                const uint8_t* Ab = Abuf + (b * NSPLIT + sa) * A_BYTES;
+                const uint8_t* Bb = Bbuf + (b * NSPLIT + sb) * b_bytes;
+                const uint64_t ad = tc_desc(Ab, 128, 256);
+                const bool acc = ks > 0 || q > 0;
+                tc_mma_f16(tmem, ad, tc_desc(Bb, 128, 256), tc_idesc_f16(FMT, 128, nt0), acc);
+                if (nt1 > 0)
+                    tc_mma_f16(tmem + 256, ad, tc_desc(Bb + (nt0 / 8) * 256, 128, 256), tc_idesc_f16(FMT, 128, nt1),
+                               acc);
+            }
+            tc_commit(&bar[b]);
+        }
+        ++use[b];
+    }
+    // wait for the last steps' MMAs (bounded; on failure still wait for work in flight)
+    for (int b = 0; b < 2 && ok; ++b)
+        if (use[b] > 0) {
+            const bool mine = mbar_wait_bounded(&bar[b], (use[b] - 1) & 1, p.err, 6);
+            ok = __syncthreads_or(mine ? 0 : 1) == 0;
+        }
+    if (!ok) {
+        for (int b = 0; b < 2; ++b)
+            if (use[b] > 0) mbar_wait_bounded(&bar[b], (use[b] - 1) & 1, p.err, 7);
+    }
+    tc_fence_after();
+    if (ok) {
+        // epilogue: warp w reads lanes 32 (w % 4) ..; warps 0-3 the first half of the Doppler
+        // bins, warps 4-7 the second
+        const int sp = warp & 3, grp = warp >> 2;
+        const int mrow = sp * 32 + lane;
+        const int col = c0 + mrow;
+        const bool valid = col < p.spc;
+        const int kh = (p.nd + 1) / 2;
+        const int kbeg = grp == 0 ? 0 : kh, kend = grp == 0 ? kh : p.nd;
+        const float inv_s2 = 1.0f / (p.scale * p.scale);
+        float* ap = p.acc + static_cast<int64_t>(pi) * p.nd * p.spc_eff;
+        const int half = p.nd / 2;
+        for (int k0 = kbeg & ~3; k0 < kend; k0 += 4) {
+            float r8[8];
+            tc_ld8(tmem + (static_cast<uint32_t>(sp * 32) << 16) + 2 * k0, r8);
+            tc_wait_ld();
+            int64_t idx[4];
+            float pw[4];
+            bool keep[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = k0 + j;
+                keep[j] = valid && k >= kbeg && k < kend;
+                pw[j] = __fadd_rn(__fmul_rn(r8[2 * j], r8[2 * j]), __fmul_rn(r8[2 * j + 1], r8[2 * j + 1])) * inv_s2;
+                int row = k + half;
+                row = row >= p.nd ? row - p.nd : row;
+                int dc = col + (keep[j] && p.has_drift ? p.drift[row] : 0);
+                dc = dc >= p.spc ? dc - p.spc : dc;
+                idx[j] = static_cast<int64_t>(row) * p.spc_eff + dc;
+            }
+            float old[4];
+            if (!p.first) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) old[j] = keep[j] ? ap[idx[j]] : 0.f;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (keep[j]) ap[idx[j]] = p.first ? pw[j] : __fadd_rn(old[j], pw[j]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tc_dealloc(tmem, 512);
+}
+
+// Real-form DFT matrix chunks for k_col_dft_mma: B[n = 2k + co][kk = 2g + ci] with
+// (co, ci) = (re, re) cos, (re, im) sin, (im, re) -sin, (im, im) cos of 2 pi g k / ndop,
+// rounded to FP16/BF16 (hi) and the rounding residual (lo), in the canonical K-major chunk
+// layout of each 16-wide K step.
+template <int FMT>
+__global__ void k_dft_operand(int nd, int n_pad, int ksteps, int nsplit, uint8_t* __restrict__ out) {
+    const int64_t total = static_cast<int64_t>(ksteps) * n_pad * 16;
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+         e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int ks = static_cast<int>(e / (n_pad * 16));
+        const int rem = static_cast<int>(e - static_cast<int64_t>(ks) * n_pad * 16);
+        const int n = rem / 16, kl = rem - (rem / 16) * 16;
+        const int k = n >> 1, co = n & 1;
+        const int g = 8 * ks + (kl >> 1), ci = kl & 1;
+        double v = 0.0;
+        if (k < nd && g < nd) {
+            double sn, cs;
+            sincospi(2.0 * static_cast<double>((static_cast<int64_t>(g) * k) % nd) / nd, &sn, &cs);
+            v = co == ci ? cs : (co == 0 ? sn : -sn);
+        }
+        const int off = (n >> 3) * 256 + (kl >> 3) * 128 + (n & 7) * 16 + (kl & 7) * 2;
+        const float vf = static_cast<float>(v);
+        const uint16_t hi = to16<FMT>(vf);
+        *reinterpret_cast<uint16_t*>(out + static_cast<int64_t>(ks) * n_pad * 32 + off) = hi;
+        if (nsplit == 2) {
+            const float h = FMT == 0 ? __half2float(__ushort_as_half(hi)) : __bfloat162float(__ushort_as_bfloat16(hi));
+            const uint16_t lo = to16<FMT>(static_cast<float>(v - static_cast<double>(h)));
+            *reinterpret_cast<uint16_t*>(out + (static_cast<int64_t>(ksteps) + ks) * n_pad * 32 + off) = lo;
+        }
+    }
+}
+
+}  // namespace acq

@@ -228,6 +228,11 @@ struct acq_plan {
     RotMmaFn rot_mma = nullptr;
     size_t smem_mma = 0;
     int rot_prec = ACQ_PREC_FP32;
+    // tensor-core Doppler DFT of the simple path (ACQ_OPT_DOPPLER_PRECISION != FP32)
+    DftMmaFn dft_mma = nullptr;
+    DevBuf dftB;
+    int dftNpad = 0, dftKsteps = 0, dft_prec = ACQ_PREC_FP32;
+    size_t smem_dft = 0;
     int mma_scale_log2 = 127;   // 127: by input type
     int Wrsb = 8, threads_rsb = 256;
     // warp-per-column sign / rotation stage
@@ -692,7 +697,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         t_end(P);
         ++L;
     }
-    const bool use_tma = !use_fused && P->col_tma != nullptr;
+    const bool use_tma = !use_fused && P->col_tma != nullptr && P->dft_mma == nullptr;
     if (use_tma) {
         // coherent tiles of every step in one launch, then the TMA-staged column stage
         const int nprn = static_cast<int>(P->prns.size());
@@ -731,7 +736,17 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         const int first = m == 0;
         const bool last = m == g.n_nc - 1;
         t_begin(P, ACQ_KERNEL_COLUMN);
-        if (g.path == 0 && P->col_fs) {
+        if (g.path == 0 && P->dft_mma) {
+            DftMmaParams dp{};
+            dp.T = P->T.as<float2>(); dp.spc = g.spc; dp.nd = g.ndop; dp.spc_eff = g.spc_eff; dp.n_pad = P->dftNpad;
+            dp.ksteps = P->dftKsteps; dp.first = first; dp.has_drift = P->step_has_drift[m]; dp.drift = dr;
+            dp.acc = P->accb.as<float>(); dp.B = P->dftB.as<uint8_t>();
+            int sl = P->mma_scale_log2;
+            if (sl == 127) sl = dtype == ACQ_CI16 ? -10 : dtype == ACQ_CI8 ? -2 : 0;
+            dp.scale = std::ldexp(1.0f, sl);
+            dp.err = P->errflag.as<int>();
+            P->dft_mma<<<dim3((g.spc + kDftCols - 1) / kDftCols, n), kDftThreads, P->smem_dft, st>>>(dp);
+        } else if (g.path == 0 && P->col_fs) {
             const int W = P->Wfs;
             P->col_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_col_fs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, dr, first, P->step_has_drift[m], P->accb.as<float>(),
@@ -1130,7 +1145,8 @@ int acq_plan_destroy(acq_plan* P) {
     if (P->stream) cudaStreamSynchronize(P->stream);
     for (DevBuf* b : {&P->twF, &P->twD, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
                       &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
-                      &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted})
+                      &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted,
+                      &P->dftB})
         b->reset();
     for (cudaEvent_t e : P->ev_start) cudaEventDestroy(e);
     for (cudaEvent_t e : P->ev_stop) cudaEventDestroy(e);
@@ -1323,6 +1339,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
         switch (option) {
             case ACQ_OPT_FORM: *value = (P->fused && P->form == ACQ_FORM_FUSED) ? ACQ_FORM_FUSED : ACQ_FORM_PLAIN; break;
             case ACQ_OPT_ROTATION_PRECISION: *value = P->rot_prec; break;
+            case ACQ_OPT_DOPPLER_PRECISION: *value = P->dft_prec; break;
             case ACQ_OPT_MMA_SCALE_LOG2: *value = P->mma_scale_log2; break;
             case ACQ_OPT_TILE_THREADS: *value = P->tile_fs ? P->tileThreads : 0; break;
             case ACQ_OPT_TILE_BLOCKS: *value = P->tile_fs ? P->tileNF : 0; break;
@@ -1402,6 +1419,44 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             setup_col_tma(P, P->n_plan_prns, W, cps);
             if (!P->col_tma) setup_col_tma(P, P->n_plan_prns, oldW, oldc);   // keep the previous shape
             if (effective) *effective = option == ACQ_OPT_COLUMN_WIDTH ? P->tmaW : P->tmaCtasPerSm;
+            return;
+        }
+        if (option == ACQ_OPT_DOPPLER_PRECISION) {
+            if (value < ACQ_PREC_FP32 || value > ACQ_PREC_BF16_SPLIT)
+                throw AcqError(ACQ_ERR_ARGUMENT, "unknown precision " + std::to_string(value));
+            const Geometry& g = P->g;
+            CK(cudaStreamSynchronize(P->stream));
+            P->dft_mma = nullptr;
+            P->dft_prec = ACQ_PREC_FP32;
+            if (value != ACQ_PREC_FP32 && g.path == 0 && g.ndop <= 250 && !getenv_flag("ACQ_GENERIC_FFT")) {
+                const int fmt = (value == ACQ_PREC_BF16 || value == ACQ_PREC_BF16_SPLIT) ? 1 : 0;
+                const int nsplit = (value == ACQ_PREC_FP16_SPLIT || value == ACQ_PREC_BF16_SPLIT) ? 2 : 1;
+                const int npad = (2 * g.ndop + 15) / 16 * 16;
+                const int ksteps = npad / 16;
+                P->dftB.ensure((size_t)nsplit * ksteps * npad * 32);
+                const int64_t total = (int64_t)ksteps * npad * 16;
+                const unsigned grid = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096));
+                if (fmt == 0)
+                    k_dft_operand<0><<<grid, 256, 0, P->stream>>>(g.ndop, npad, ksteps, nsplit, P->dftB.as<uint8_t>());
+                else
+                    k_dft_operand<1><<<grid, 256, 0, P->stream>>>(g.ndop, npad, ksteps, nsplit, P->dftB.as<uint8_t>());
+                CK(cudaGetLastError());
+                CK(cudaStreamSynchronize(P->stream));
+                DftMmaFn fn = fmt == 0 ? (nsplit == 2 ? &k_col_dft_mma<0, 2> : &k_col_dft_mma<0, 1>)
+                                       : (nsplit == 2 ? &k_col_dft_mma<1, 2> : &k_col_dft_mma<1, 1>);
+                // one block per SM (the block holds 512 TMEM columns)
+                const size_t need = 1024 + 2 * (size_t)nsplit * 4096 + 2 * (size_t)nsplit * npad * 32 + 64;
+                const size_t smem = std::max<size_t>(need, 120 * 1024);
+                set_smem((const void*)fn, smem);
+                P->errflag.ensure(sizeof(int));
+                CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
+                P->dft_mma = fn;
+                P->smem_dft = smem;
+                P->dftNpad = npad;
+                P->dftKsteps = ksteps;
+                P->dft_prec = static_cast<int>(value);
+            }
+            if (effective) *effective = P->dft_prec;
             return;
         }
         if (option == ACQ_OPT_MMA_SCALE_LOG2) {

@@ -722,22 +722,24 @@ def main():
     ktimes = plan.kernel_times()
     plan.set_kernel_timing(False)
 
-    # ---- rotation searches: the combine on the tensor cores (FP16/BF16, single or split hi + lo)
-    # against the FP32 path: throughput, power error relative to the FP32 surface's peak on
-    # two PRNs (strongest planted, one absent) and agreement of every PRN's decisions
+    # ---- tensor-core variants against the FP32 path: rotation searches (the candidate combine)
+    # and the simple path (the per-column Doppler DFT as a DFT-matrix GEMM, ndop <= 250):
+    # throughput, power error relative to the FP32 surface's peak on two PRNs (strongest planted,
+    # one absent) and agreement of every PRN's decisions
     study = None
-    if plan.geometry.path == 2 and not args.no_precision_study:
-        study = {}
-        base_prec = main_prec
+    gpath = plan.geometry.path
+    if not args.no_precision_study and (gpath == 2 or (gpath == 0 and plan.geometry.num_doppler_bins <= 250)):
+        setter = plan.set_rotation_precision if gpath == 2 else plan.set_doppler_precision
+        study = {"stage": "rotation combine" if gpath == 2 else "Doppler DFT (dense DFT-matrix GEMM)"}
         strong = max(sats, key=lambda s_: s_.cn0).prn
         absent = next(p_ for p_ in PRNS if p_ not in {s_.prn for s_ in sats})
-        pair = [strong, absent]
-        plan.set_rotation_precision("fp32")
+        pair = [q for q in (strong, absent) if q in PRNS]
+        setter("fp32")
         ref_all = A.acquire_device(plan, dev, PRNS)
-        ref_pb = {r.prn: np.asarray(r.power_bins, dtype=np.float64)
+        ref_pb = {r.prn: np.asarray(r.power_bins, dtype=np.float64).copy()
                   for r in A.acquire_b(plan, host_np, pair, store_power_bins=True)}
         for prec in ("fp32", "fp16", "bf16", "fp16_split", "bf16_split"):
-            if plan.set_rotation_precision(prec) != prec:
+            if setter(prec) != prec:
                 continue
             A.acquire_device(plan, dev, PRNS)
             pm = []
@@ -758,7 +760,7 @@ def main():
             err = max(float(np.max(np.abs(pb[q] - ref_pb[q])) / np.max(ref_pb[q])) for q in pair)
             study[prec] = {"value": world * 1e3 / statistics.mean(pm), "unit": "acq/s",
                            "max_power_error_vs_fp32": err, "prns_with_same_decisions": same}
-        plan.set_rotation_precision(base_prec)
+        setter(args.precision if gpath == 2 else "fp32")
 
     # ---- e2e: public API, pinned host input, H2D + compute + D2H inside the timed region
     e2e_s = []

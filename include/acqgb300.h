@@ -176,6 +176,8 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_OPT_TILE_PAD 5           /*   shared-memory padding between FFT buffers, complex elements (0..32) */
 #define ACQ_OPT_COLUMN_WIDTH 6       /* TMA column kernel: code-phase columns per tile (8, 16, 32) */
 #define ACQ_OPT_COLUMN_CTAS_PER_SM 7 /*   persistent CTAs per SM (1..occupancy limit) */
+#define ACQ_OPT_DOPPLER_PRECISION 8  /* simple path: the per-column Doppler DFT as a dense DFT-matrix GEMM on the
+                                        tensor cores (ACQ_PREC_*; ndop <= 250), or FP32 FFTs (default) */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
  * form is used only where the plan's sizes have a fused kernel (otherwise plain).
