@@ -78,7 +78,8 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_batch_create", "acq_batch_destroy", "acq_batch_input_ptr", "acq_batch_upload", "acq_batch_launch",
             "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
             "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine",
-            "acq_plan_get_option", "acq_chip_order", "acq_sort_power_bins_by_chip", "acq_gen_code_device"]
+            "acq_plan_get_option", "acq_chip_order", "acq_sort_power_bins_by_chip", "acq_gen_code_device",
+            "acq_selftest_bounded_wait"]
 ACQ_OPT_FORM = 0
 ACQ_OPT_ROTATION_PRECISION = 1
 ACQ_OPT_MMA_SCALE_LOG2 = 2
@@ -131,6 +132,7 @@ def load():
     lib.acq_chip_order.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.c_double, C.c_double, C.POINTER(C.c_int32),
                                    C.POINTER(C.c_double)]
     lib.acq_sort_power_bins_by_chip.argtypes = [P, P, C.c_int32, P, P]
+    lib.acq_selftest_bounded_wait.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_int32)]
     lib.acq_gen_code_device.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_int64, C.c_double,
                                         C.c_double, C.c_double, P, P]
     lib.acq_corr_create.argtypes = [C.c_int32, C.c_double, C.POINTER(C.c_int32), C.c_int32, C.POINTER(C.c_int8),

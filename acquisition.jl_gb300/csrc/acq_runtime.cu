@@ -83,6 +83,18 @@ void sample_codes_device(int system, const int8_t* d_chips, int64_t L, int n_prn
     CK(cudaGetLastError());
 }
 
+// Bounded-wait self test: an mbarrier that nothing arrives on; the wait must give up after
+// `polls` polls and record code 9, leaving the context usable.
+__global__ void k_wait_selftest(uint32_t polls, int* err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    mbar_wait_bounded(&bar, 0, err, 9, polls);
+}
+
 // out[r][i] = in[r][perm[i]] for rows of `width` columns (chip-sorted power surfaces)
 __global__ void k_gather_cols(const float* __restrict__ in, int64_t rows, int64_t width, const int32_t* __restrict__ perm,
                               float* __restrict__ out) {
@@ -1501,6 +1513,25 @@ int acq_gen_code_device(int32_t system, const int32_t* prns, int32_t n_prns, int
         sample_codes_device(system, d_chips, L, n_prns, n, fs, fc, start_phase, d_out, st);
         CK(cudaFreeAsync(d_chips, st));
         CK(cudaStreamSynchronize(st));   // the host chip tables go out of scope
+    });
+}
+
+int acq_selftest_bounded_wait(int32_t device, uint32_t polls, int32_t* status) {
+    return guarded([&] {
+        if (!status) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (polls < 1 || polls > (1u << 26)) throw AcqError(ACQ_ERR_ARGUMENT, "polls must be in 1:2^26");
+        CK(cudaSetDevice(device));
+        int* d_err = nullptr;
+        CK(cudaMalloc(&d_err, sizeof(int)));
+        CK(cudaMemset(d_err, 0, sizeof(int)));
+        k_wait_selftest<<<1, 32>>>(polls, d_err);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        int h = 0;
+        if (e == cudaSuccess) e = cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+        cudaFree(d_err);
+        if (e != cudaSuccess) throw CudaError(std::string("self test: ") + cudaGetErrorString(e));
+        *status = h == 9 ? ACQ_ERR_TIMEOUT : ACQ_OK;
     });
 }
 

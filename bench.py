@@ -389,6 +389,16 @@ def run_batch(args, world, rank, local_rank):
     print(json.dumps(line))
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's time (replicas: the job ends when the last one does)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 FINE_FLOPS = {"eval": 34, "hess": 56, "vjp": 19}   # FP32 flops per (cell, sample), see run_fine
 
 
@@ -675,11 +685,7 @@ def main():
             ev_ms.append(e0.elapsed_time(e1))
         barrier()
     clocks = clk.summary()
-    t_step = statistics.mean(ev_ms) / 1e3
-    if dist is not None:
-        t = torch.tensor([t_step], device=f"cuda:{local_rank}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
+    t_step = max_over_ranks(statistics.mean(ev_ms) / 1e3, dist, f"cuda:{local_rank}")
     value = world * 1.0 / t_step
 
     # ---- the other form on the same input (plain: one kernel per stage, tile and accumulator
@@ -769,11 +775,7 @@ def main():
         t0 = time.perf_counter()
         A.acquire_b(plan, host_np, PRNS)
         e2e_s.append(time.perf_counter() - t0)
-    t_e2e = statistics.mean(e2e_s)
-    if dist is not None:
-        t = torch.tensor([t_e2e], device=f"cuda:{local_rank}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(statistics.mean(e2e_s), dist, f"cuda:{local_rank}")
     e2e_value = world / t_e2e
 
     if rank != 0:

@@ -263,6 +263,12 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_in
 int acq_gen_code_device(int32_t system, const int32_t* prns, int32_t n_prns, int64_t n, double sampling_freq_hz,
                         double code_freq_hz, double start_phase, int8_t* d_out, void* stream);
 
+/* Failure-detection self test: one block waits (bounded, `polls` polls) on an mbarrier that
+ * nothing arrives on, the way every device wait of the library is bounded. *status =
+ * ACQ_ERR_TIMEOUT when the wait gave up and reported it (the expected outcome), ACQ_OK otherwise;
+ * the context stays usable. */
+int acq_selftest_bounded_wait(int32_t device, uint32_t polls, int32_t* status);
+
 /* Column order of a power surface sorted by code phase, src/plot.jl:16-20,35-57 (host, no GPU):
  * perm[i] = the FM-DBZP column at chip-sorted position i (width entries), chip_axis[i] (may be
  * NULL) its code phase in chips, monotone. width = the surface's columns (samples_per_code_eff). */

@@ -180,3 +180,15 @@ def test_column_to_tau_known_answers():
     assert [O.fmdbzp_column_to_tau(c, 4, 8) for c in (0, 1, 8, 16, 24)] == [0, 1, 24, 16, 8]
     assert O.fmdbzp_column_to_tau(0, 32, 64) == 0
     assert sorted(O.fmdbzp_column_to_tau(c, 4, 8) for c in range(32)) == list(range(32))
+
+
+def test_bounded_wait_selftest_fails_loudly_without_gpu():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    st = C.c_int32(-1)
+    assert L.load().acq_selftest_bounded_wait(0, 1000, C.byref(st)) == L.ACQ_ERR_CUDA
+    assert L.load().acq_selftest_bounded_wait(0, 0, C.byref(st)) == L.ACQ_ERR_ARGUMENT
