@@ -59,6 +59,11 @@ class Result(C.Structure):
                 ("detected", C.c_int32), ("reserved", C.c_int32)]
 
 
+class SynthSat(C.Structure):
+    _fields_ = [("prn", C.c_int32), ("data_bits", C.c_int32), ("cn0_dbhz", C.c_double), ("doppler_hz", C.c_double),
+                ("code_phase", C.c_double), ("carrier_phase", C.c_double), ("bit_offset_s", C.c_double)]
+
+
 class CorrCell(C.Structure):
     _fields_ = [("prn", C.c_int32), ("reserved", C.c_int32), ("code_phase", C.c_double), ("doppler_hz", C.c_double)]
 
@@ -79,7 +84,7 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
             "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine",
             "acq_plan_get_option", "acq_chip_order", "acq_sort_power_bins_by_chip", "acq_gen_code_device",
-            "acq_selftest_bounded_wait"]
+            "acq_selftest_bounded_wait", "acq_synth_signal"]
 ACQ_OPT_FORM = 0
 ACQ_OPT_ROTATION_PRECISION = 1
 ACQ_OPT_MMA_SCALE_LOG2 = 2
@@ -132,6 +137,8 @@ def load():
     lib.acq_chip_order.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.c_double, C.c_double, C.POINTER(C.c_int32),
                                    C.POINTER(C.c_double)]
     lib.acq_sort_power_bins_by_chip.argtypes = [P, P, C.c_int32, P, P]
+    lib.acq_synth_signal.argtypes = [C.c_int32, C.c_double, C.c_int64, C.POINTER(SynthSat), C.c_int32, C.c_double,
+                                     C.c_uint64, C.c_int32, C.c_int32, P, P]
     lib.acq_selftest_bounded_wait.argtypes = [C.c_int32, C.c_uint32, C.POINTER(C.c_int32)]
     lib.acq_gen_code_device.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.c_int32, C.c_int64, C.c_double,
                                         C.c_double, C.c_double, P, P]

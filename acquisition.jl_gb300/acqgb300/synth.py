@@ -130,3 +130,29 @@ def ragged_batch(seed: int = 3, n_recordings: int = 64, n_antennas: int = 4, max
         out.append(dict(system=sysm, fs=fs, samples=x, prns=sorted(int(p) for p in searched), n_coh=n_coh,
                         n_nc=n_nc, cov=8000.0, sats=sats, antenna=ant, length_ms=length_ms))
     return out
+
+
+def synth_device(system: GNSSSystem, fs: float, n: int, sats, seed: int, *, interm_freq: float = 0.0,
+                 noise: bool = True, dtype: str = "cf32", out=None, stream: int = 0):
+    """The same signal model generated on the GPU (``acq_synth_signal``) into a CUDA tensor (or
+    ``out``: a device pointer or tensor). Data bits and noise come from a counter-based generator
+    (not numpy's stream); the code and carrier match :func:`synth`."""
+    import ctypes as C
+    import torch
+    from . import _lib as L
+    from .api import _check
+    code = {"cf32": L.ACQ_CF32, "ci16": L.ACQ_CI16, "ci8": L.ACQ_CI8, "cf64": L.ACQ_CF64}[dtype]
+    arr = (L.SynthSat * max(1, len(sats)))()
+    for i, s in enumerate(sats):
+        arr[i] = L.SynthSat(int(s.prn), 1 if s.data_bits else 0, float(s.cn0), float(s.doppler), float(s.code_phase),
+                            float(s.phase), float(s.bit_offset))
+    if out is None:
+        out = {"cf32": lambda: torch.empty(n, dtype=torch.complex64, device="cuda"),
+               "cf64": lambda: torch.empty(n, dtype=torch.complex128, device="cuda"),
+               "ci16": lambda: torch.empty((n, 2), dtype=torch.int16, device="cuda"),
+               "ci8": lambda: torch.empty((n, 2), dtype=torch.int8, device="cuda")}[dtype]()
+    ptr = out.data_ptr() if hasattr(out, "data_ptr") else int(out)
+    _check(L.load().acq_synth_signal(system.sid, float(fs), int(n), arr, len(sats), float(interm_freq),
+                                     int(seed) & 0xFFFFFFFFFFFFFFFF, 1 if noise else 0, code, C.c_void_p(ptr),
+                                     C.c_void_p(stream)))
+    return out

@@ -46,6 +46,7 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
     dev_obj = os.path.join(BUILD_DIR, "acq_runtime.o")
     na_obj = os.path.join(BUILD_DIR, "acq_noalloc.o")
     corr_obj = os.path.join(BUILD_DIR, "acq_corr.o")
+    synth_obj = os.path.join(BUILD_DIR, "acq_synth.o")
     inst = ["acq_inst_tile", "acq_inst_col", "acq_inst_sign", "acq_inst_mma"]
     inst_objs = [os.path.join(BUILD_DIR, f"{n}.o") for n in inst]
     host_cmd = ["g++", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", *opt,
@@ -56,6 +57,8 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
               f"-I{INCLUDE}", f"-I{CSRC}", "-c", os.path.join(CSRC, "acq_noalloc.cu"), "-o", na_obj]
     corr_cmd = [nvcc, "-std=c++17", *ARCH, "-lineinfo", *opt, "-Xcompiler", "-fPIC,-ffp-contract=off",
                 f"-I{INCLUDE}", f"-I{CSRC}", "-c", os.path.join(CSRC, "acq_corr.cu"), "-o", corr_obj]
+    synth_cmd = [nvcc, "-std=c++17", *ARCH, "-lineinfo", *opt, "-Xcompiler", "-fPIC,-ffp-contract=off",
+                 f"-I{INCLUDE}", f"-I{CSRC}", "-c", os.path.join(CSRC, "acq_synth.cu"), "-o", synth_obj]
     if ptxas_verbose:
         dev_cmd.insert(1, "-Xptxas=-v")
         corr_cmd.insert(1, "-Xptxas=-v")
@@ -65,10 +68,10 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
     if ptxas_verbose:
         for c in inst_cmds:
             c.insert(1, "-Xptxas=-v")
-    cmds = [host_cmd, dev_cmd, na_cmd, corr_cmd, *inst_cmds]
+    cmds = [host_cmd, dev_cmd, na_cmd, corr_cmd, synth_cmd, *inst_cmds]
     with ThreadPoolExecutor(len(cmds)) as ex:
         outs = list(ex.map(_run, cmds))
-    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, na_obj, corr_obj, *inst_objs, "-o", LIB + ".tmp", "-lcudart_static", "-lrt", "-ldl",
+    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, na_obj, corr_obj, synth_obj, *inst_objs, "-o", LIB + ".tmp", "-lcudart_static", "-lrt", "-ldl",
                 "-lpthread"]
     outs.append(_run(link_cmd))
     os.replace(LIB + ".tmp", LIB)

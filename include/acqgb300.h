@@ -263,6 +263,25 @@ int acq_cfar_threshold(double pfa, int64_t num_cells, int32_t num_noncoherent_in
 int acq_gen_code_device(int32_t system, const int32_t* prns, int32_t n_prns, int64_t n, double sampling_freq_hz,
                         double code_freq_hz, double start_phase, int8_t* d_out, void* stream);
 
+/* ---- synthetic recordings on the device (src/generate_test_signal.jl:32-82) ---- */
+typedef struct {
+    int32_t prn;
+    int32_t data_bits;        /* 1: +-1 data bits at the system's data rate (counter-based random values) */
+    double cn0_dbhz;          /* amplitude sqrt(10^(CN0/10) / fs) for unit noise power */
+    double doppler_hz;        /* carrier Doppler; the code runs at f_code + f_d f_code / f_carrier */
+    double code_phase;        /* chips at sample 0 */
+    double carrier_phase;     /* rad */
+    double bit_offset_s;      /* time into the first data bit at sample 0 */
+} acq_synth_sat;              /* 48 bytes */
+
+/* Write n samples of `dtype` (ACQ_CF32 / CI16 / CI8 / CF64) to device memory d_out: the sum of the
+ * satellites' signals (code with gen_code semantics, carrier, data bits) plus, when noise != 0,
+ * complex white Gaussian noise of unit power from a counter-based generator seeded by `seed`.
+ * CI16 = round(x 2^10) saturated; CI8 = 3-bit quantiser (odd levels, step 0.5 sigma). Waits for
+ * `stream` before returning. */
+int acq_synth_signal(int32_t system, double sampling_freq_hz, int64_t n, const acq_synth_sat* sats, int32_t n_sats,
+                     double interm_freq_hz, uint64_t seed, int32_t noise, int32_t dtype, void* d_out, void* stream);
+
 /* Failure-detection self test: one block waits (bounded, `polls` polls) on an mbarrier that
  * nothing arrives on, the way every device wait of the library is bounded. *status =
  * ACQ_ERR_TIMEOUT when the wait gave up and reported it (the expected outcome), ACQ_OK otherwise;
