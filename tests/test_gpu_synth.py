@@ -69,3 +69,12 @@ def test_ragged_batch_fed_from_the_device_generator():
         r = {x.prn: x for x in res}[sat.prn]
         assert A.is_detected(r), (system.name, sat.prn)
         assert abs(r.carrier_doppler - sat.doppler) <= p.geometry.doppler_step_hz
+
+
+def test_recommendation_with_measured_gpu_cost():
+    from acqgb300 import recommend as R
+    rs = R.recommend_for_system(A.GPSL1CA(), fs_min=2e6, fs_max=5e6, min_doppler_coverage=7000, num_alternatives=3,
+                                measure=A.GPSL1CA(), measure_top=4)
+    assert 0 < len(rs) <= 3
+    ms = [r.measured_ms for r in rs]
+    assert all(m is not None and m > 0 for m in ms) and ms == sorted(ms)
