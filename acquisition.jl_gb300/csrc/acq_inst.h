@@ -44,9 +44,6 @@ using RotMmaFn = void (*)(RotMmaParams);
 // ACQ_PREC_* precision other than FP32; nullptr when not instantiated; *smem = dynamic bytes.
 RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec, size_t* smem);
 
-using SearchFn = void (*)(SearchParams);
-// warp-per-column search stage (mode 1 sign, 2 rotation); pc = candidates transformed together
-SearchFn pick_search_warp(int mode, int ndop, int* pc);
 
 TileFsFn pick_tile_fs(int fft_size);
 FusedFn pick_fused(int fft_size, int ndop);

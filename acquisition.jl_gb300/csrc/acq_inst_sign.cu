@@ -24,16 +24,6 @@ RotFsFn pick_rot_fs(int ndop) {
     }
 }
 
-// PC = 32 / N1 candidates per warp pass fill the lanes of the second FFT pass.
-#define ACQ_SW_CASE(MODE, N)                                                                   \
-    if (ndop == N) {                                                                           \
-        constexpr int n1 = best_split_n1(N), n2 = N / best_split_n1(N);                        \
-        constexpr int pcv = (32 / n1) > 0 ? (32 / n1 > 4 ? 4 : 32 / n1) : 1;                   \
-        *pc = pcv;                                                                             \
-        return &k_col_search_warp<n1, n2, MODE, pcv>;                                          \
-    }
-
-// 16 columns per block up to 384 Doppler bins (wider coalesced accumulator rows), else 8
 #define ACQ_RSB_CASE(NC, NB)                                                \
     if (n_coh == NC && nb == NB) {                                          \
         constexpr int kW = (NC * NB <= 384) ? 16 : 8;                       \
@@ -59,17 +49,6 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
 SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {
     ACQ_SSB_CASE(32, 25, 8, 2) ACQ_SSB_CASE(32, 20, 8, 2) ACQ_SSB_CASE(32, 40, 4, 2) ACQ_SSB_CASE(20, 20, 8, 2)
     ACQ_SSB_CASE(16, 25, 8, 1) ACQ_SSB_CASE(20, 10, 16, 2)
-    return nullptr;
-}
-
-SearchFn pick_search_warp(int mode, int ndop, int* pc) {
-    if (mode == 2) {
-        ACQ_SW_CASE(2, 40) ACQ_SW_CASE(2, 100) ACQ_SW_CASE(2, 120) ACQ_SW_CASE(2, 160) ACQ_SW_CASE(2, 200)
-        ACQ_SW_CASE(2, 240) ACQ_SW_CASE(2, 250) ACQ_SW_CASE(2, 400) ACQ_SW_CASE(2, 500)
-    } else {
-        ACQ_SW_CASE(1, 40) ACQ_SW_CASE(1, 200) ACQ_SW_CASE(1, 400) ACQ_SW_CASE(1, 500) ACQ_SW_CASE(1, 640)
-        ACQ_SW_CASE(1, 800)
-    }
     return nullptr;
 }
 

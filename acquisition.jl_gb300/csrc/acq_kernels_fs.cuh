@@ -919,161 +919,4 @@ __global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W)
     scatter_rmw<W>(stg, wst, ND * W, tid, blockDim.x, wv, c0, spc, spc_eff, 0, drift, first, ap, wp);
 }
 
-// ------------------------------------------------------------------ warp-per-column search stage
-// Sign (MODE 1) or rotation (MODE 2) search with one warp per code-phase column: the CTA loads an
-// (ndop x 8) tile once, then every warp runs all candidates of its column with warp-level sync
-// only, PC candidates at a time (PC two-pass FFTs side by side fill the lanes when ndop is small)
-// and merges them into its private stage in candidate order (strict >, earlier candidate keeps
-// ties), exactly the order of src/noncoherent_integration.jl:60-115 / :183-297 and :654-686.
-// One block barrier per stage slice writes the 8 columns to the accumulator coalesced.
-struct SearchParams {
-    const float2* T;
-    int spc, spc_eff;
-    const float2* twD;
-    const float* pats;       // per slot: n_pat x n_coh
-    int n_pat, n_coh, ndb, n_be, edge_step;
-    int nb, bs, R, combos, use_max;
-    const int* slots;
-    const int* drift;
-    int first;
-    float* acc;
-    uint16_t* win;
-};
-
-template <int N1, int N2, int MODE, int PC>
-__global__ void __launch_bounds__(256) k_col_search_warp(SearchParams sp) {
-    constexpr int ND = N1 * N2;
-    constexpr int TW = 8;                      // columns per CTA = warps per CTA
-    constexpr int half = ND / 2;
-    extern __shared__ float2 sm[];
-    float2* tile = sm;                                       // ND x TW
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    float2* wk = tile + ND * TW + wid * (PC * ND);           // PC work vectors of this warp
-    float* pwb = reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) + wid * (PC * ND);
-    float* stage = reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) + TW * PC * ND + wid * ND;
-    uint16_t* wst = reinterpret_cast<uint16_t*>(reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) +
-                                                TW * PC * ND + TW * ND) + wid * ND;
-    const int pi = blockIdx.y;
-    const int slot = sp.slots[pi];
-    const int c0 = blockIdx.x * TW;
-    const int wv = min(TW, sp.spc - c0);
-    const float2* tp = sp.T + static_cast<int64_t>(pi) * ND * sp.spc;
-    for (int w = threadIdx.x; w < ND * TW; w += blockDim.x) {
-        const int e = w / TW, t = w - e * TW;
-        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * sp.spc + c0 + t] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    const int t = wid;                                        // this warp's column within the tile
-    int cro = 0;
-    if (MODE == 2) {
-        const int pc = c0 + t;
-        const int wrap = ((sp.nb - pc / sp.bs) % sp.nb) * sp.bs + pc % sp.bs;   // src/noncoherent_integration.jl:212-214
-        cro = ((wrap + (sp.bs >> 1)) / sp.bs) % sp.nb;
-    }
-    const float* pp = sp.pats + static_cast<int64_t>(slot) * sp.n_pat * sp.n_coh;
-    const int n_slices = MODE == 2 ? sp.R : 1;
-    const int per_slice = MODE == 2 ? sp.n_be * sp.combos : sp.n_be * sp.n_pat;
-    const int sub_len = ND / sp.ndb;
-    const int coh_per_bit = sp.n_coh / sp.ndb;
-    const bool use_max = MODE == 1 || sp.use_max != 0;
-    float* ap = sp.acc + static_cast<int64_t>(pi) * ND * sp.spc_eff;
-    uint16_t* wp = sp.win + static_cast<int64_t>(pi) * ND * sp.spc_eff;
-    for (int s = 0; s < n_slices; ++s) {
-        if (t < wv) {
-            for (int i = lane; i < ND; i += 32) {
-                stage[i] = 0.f;
-                wst[i] = 0;
-            }
-            for (int cb = 0; cb < per_slice; cb += PC) {
-                const int pc_n = min(PC, per_slice - cb);
-                // ---- build the candidate vectors
-                for (int u = 0; u < pc_n; ++u) {
-                    const int c = cb + u;
-                    float2* x = wk + u * ND;
-                    if (MODE == 2) {
-                        const int e = c / sp.combos, d = c - e * sp.combos;
-                        const float* pq = pp + static_cast<int64_t>(s * sp.combos + d) * sp.n_coh;
-                        const int eff = (e * sp.edge_step + cro) % ND;
-                        for (int i = lane; i < ND; i += 32) {
-                            int row = eff + i;
-                            if (row >= ND) row -= ND;
-                            const float sg = pq[i / sp.nb];
-                            const float2 v = tile[row * TW + t];
-                            x[i] = make_float2(sg * v.x, sg * v.y);
-                        }
-                    } else {
-                        const int e = c / sp.n_pat, p = c - e * sp.n_pat;
-                        const int row_offset = e * sp.edge_step;
-                        for (int i = lane; i < ND; i += 32) {
-                            float2 v = make_float2(0.f, 0.f);
-                            if (i < sub_len) {
-                                for (int b = 0; b < sp.ndb; ++b) {
-                                    const float sg = pp[p * sp.n_coh + b * coh_per_bit];
-                                    const float2 y = tile[((row_offset + b * sub_len + i) % ND) * TW + t];
-                                    v = make_float2(v.x + sg * y.x, v.y + sg * y.y);
-                                }
-                            }
-                            x[i] = v;
-                        }
-                    }
-                }
-                __syncwarp();
-                for (int task = lane; task < pc_n * N2; task += 32) {
-                    const int u = task / N2, n2 = task - u * N2;
-                    fourstep_pass1<N1, N2, false>(wk + u * ND, 1, n2, sp.twD);
-                }
-                __syncwarp();
-                for (int task = lane; task < pc_n * N1; task += 32) {
-                    const int u = task / N1, k1 = task - u * N1;
-                    const float2* x = wk + u * ND;
-                    float2 v[N2];
-#pragma unroll
-                    for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[N2 * k1 + n2];
-                    RegFFT<N2, false>::run(v);
-                    float* pw = pwb + u * ND;
-                    static_for<0, N2>([&](auto kc) {
-                        constexpr int k2 = decltype(kc)::value;
-                        constexpr int pr = reg_perm(N2, k2);
-                        const int om = k1 + N1 * k2;
-                        const float2 xv = v[pr];
-                        pw[om < half ? om + half : om - half] =
-                            __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
-                    });
-                }
-                __syncwarp();
-                // ---- merge in candidate order
-                for (int row = lane; row < ND; row += 32) {
-                    float best = stage[row];
-                    uint16_t bw = wst[row];
-                    for (int u = 0; u < pc_n; ++u) {
-                        const float v = pwb[u * ND + row];
-                        if (!use_max || v > best) {
-                            best = v;
-                            bw = static_cast<uint16_t>(cb + u);
-                        }
-                    }
-                    stage[row] = best;
-                    wst[row] = bw;
-                }
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        // ---- coalesced scatter of the TW columns of this slice (drift wraps inside the slice)
-        float* stg0 = reinterpret_cast<float*>(tile + ND * TW + TW * PC * ND) + TW * PC * ND;
-        uint16_t* wst0 = reinterpret_cast<uint16_t*>(stg0 + TW * ND);
-        for (int w = threadIdx.x; w < ND * TW; w += blockDim.x) {
-            const int row = w / TW, tc = w - row * TW;
-            if (tc >= wv) continue;
-            int dc = c0 + tc + sp.drift[row];
-            if (dc >= sp.spc) dc -= sp.spc;
-            const int64_t idx = static_cast<int64_t>(row) * sp.spc_eff + s * sp.spc + dc;
-            const float v = stg0[tc * ND + row];
-            ap[idx] = sp.first ? v : ap[idx] + v;
-            wp[idx] = wst0[tc * ND + row];
-        }
-        __syncthreads();
-    }
-}
-
 }  // namespace acq

@@ -247,10 +247,6 @@ struct acq_plan {
     size_t smem_dft = 0;
     int mma_scale_log2 = 127;   // 127: by input type
     int Wrsb = 8, threads_rsb = 256;
-    // warp-per-column sign / rotation stage
-    SearchFn search_warp = nullptr;
-    int search_pc = 1;
-    size_t smem_search = 0;
     // specialised sign / rotation stages
     SignFsFn sign_fs = nullptr;
     RotFsFn rot_fs = nullptr;
@@ -503,21 +499,6 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
             P->smem_rsb = need;
             P->Wrsb = w;
             P->threads_rsb = th;
-        }
-    }
-    if ((g.path == 1 || g.path == 2) && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT") &&
-        getenv_flag("ACQ_WARP_SEARCH")) {
-        int pc = 1;
-        SearchFn fn = pick_search_warp(g.path, g.ndop, &pc);
-        if (fn) {
-            const size_t smem = sizeof(float2) * (size_t)g.ndop * 8 + 8 * (size_t)pc * g.ndop * (8 + 4) +
-                                8 * (size_t)g.ndop * (4 + 2) + 64;
-            if (smem <= 200 * 1024) {
-                set_smem((const void*)fn, smem);
-                P->search_warp = fn;
-                P->search_pc = pc;
-                P->smem_search = smem;
-            }
         }
     }
     if (P->sign_fs || P->rot_fs) {
@@ -778,21 +759,13 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             rp.scale = std::ldexp(1.0f, sl);
             rp.err = P->errflag.as<int>();
             P->rot_mma<<<dim3((g.spc + kRotMmaW - 1) / kRotMmaW, n), 256, P->smem_mma, st>>>(rp);
-        } else if (g.path == 2 && P->rot_sb && !P->search_warp) {
+        } else if (g.path == 2 && P->rot_sb) {
             const int W = P->Wrsb;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
             P->rot_sb<<<dim3((g.spc + W - 1) / W, n), P->threads_rsb, P->smem_rsb, st>>>(
                 P->T.as<float2>(), g.spc, P->fftD.tw, P->pats.as<float>(), g.bs, g.R, P->combos, g.n_be,
                 P->edge_step, use_max, a.d_slots, dr, first | (last ? 2 : 0), P->accb.as<float>(),
                 P->winb.as<uint16_t>(), g.spc_eff);
-        } else if (g.path != 0 && P->search_warp) {
-            SearchParams sp{};
-            sp.T = P->T.as<float2>(); sp.spc = g.spc; sp.spc_eff = g.spc_eff; sp.twD = P->fftD.tw;
-            sp.pats = P->pats.as<float>(); sp.n_pat = P->n_pat; sp.n_coh = g.n_coh; sp.ndb = g.ndb; sp.n_be = g.n_be;
-            sp.edge_step = P->edge_step; sp.nb = g.nb; sp.bs = g.bs; sp.R = g.R; sp.combos = P->combos;
-            sp.use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0; sp.slots = a.d_slots; sp.drift = dr; sp.first = first;
-            sp.acc = P->accb.as<float>(); sp.win = P->winb.as<uint16_t>();
-            P->search_warp<<<dim3((g.spc + 7) / 8, n), kThreads, P->smem_search, st>>>(sp);
         } else if (g.path == 1 && P->sign_sb) {
             const int W = P->Wssb;
             P->sign_sb<<<dim3((g.spc + W - 1) / W, n), P->threads_ssb, P->smem_ssb, st>>>(
