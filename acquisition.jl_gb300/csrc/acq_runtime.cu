@@ -1002,9 +1002,9 @@ void batch_free(acq_batch* B) {
 void fetch(acq_plan* P, acq_result* results, float* power_bins) {
     const Geometry& g = P->g;
     CK(cudaSetDevice(P->device));
-    if (results)
+    if (results && P->last_n > 0)
         CK(cudaMemcpyAsync(results, P->res.p, sizeof(acq_result) * P->last_n, cudaMemcpyDeviceToHost, P->stream));
-    if (power_bins && (P->last_flags & ACQ_FLAG_STORE_POWER_BINS)) {
+    if (power_bins && P->last_n > 0 && (P->last_flags & ACQ_FLAG_STORE_POWER_BINS)) {
         const size_t cells = (size_t)P->last_n * g.ndop * g.spc_eff;
         const void* src = P->accb.p;
         if (P->last_flags & ACQ_FLAG_POWER_BINS_CHIP_SORTED) {
@@ -1154,10 +1154,31 @@ int acq_plan_doppler_freqs(const acq_plan* P, double* out) {
     });
 }
 
+// acquire! with an empty PRN list (src/acquire.jl:54-89): the signal length is still checked,
+// then there is nothing to compute and the result list is empty.
+bool empty_request(acq_plan* P, int64_t n_samples, int32_t n_prns, uint32_t flags) {
+    if (n_prns < 0) throw AcqError(ACQ_ERR_ARGUMENT, "n_prns must be >= 0");
+    if (n_prns > 0) return false;
+    const Geometry& g = P->g;
+    const int64_t seg_len = static_cast<int64_t>(g.n_coh) * g.spc;
+    const int64_t nseg = n_samples / seg_len;
+    if (nseg < g.n_nc)
+        throw AcqError(ACQ_ERR_SHORT_SIGNAL, "Signal has " + std::to_string(n_samples) + " samples → " +
+                                                 std::to_string(nseg) + " full segments of " + std::to_string(seg_len) +
+                                                 ", but plan.num_noncoherent_accumulations=" + std::to_string(g.n_nc) +
+                                                 ". Provide a longer signal.");
+    P->last_n = 0;
+    P->last_flags = flags;
+    return true;
+}
+
 int acq_acquire(acq_plan* P, const void* samples, int32_t dtype, int64_t n_samples, const int32_t* prns,
                 int32_t n_prns, double interm_freq_hz, uint32_t flags, acq_result* results, float* power_bins) {
     return guarded([&] {
-        if (!P || !samples || !prns || !results) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (!P || !samples) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        sample_bytes(dtype);
+        if (empty_request(P, n_samples, n_prns, flags)) return;
+        if (!prns || !results) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         if ((flags & ACQ_FLAG_STORE_POWER_BINS) && !power_bins)
             throw AcqError(ACQ_ERR_ARGUMENT, "store_power_bins requested without an output buffer");
         const size_t eb = sample_bytes(dtype);
@@ -1176,8 +1197,10 @@ int acq_acquire(acq_plan* P, const void* samples, int32_t dtype, int64_t n_sampl
 int acq_acquire_device_async(acq_plan* P, const void* d_samples, int32_t dtype, int64_t n_samples,
                              const int32_t* prns, int32_t n_prns, double interm_freq_hz, uint32_t flags) {
     return guarded([&] {
-        if (!P || !d_samples || !prns) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (!P || !d_samples) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         sample_bytes(dtype);
+        if (empty_request(P, n_samples, n_prns, flags)) return;
+        if (!prns) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         enqueue_acquire(P, d_samples, dtype, n_samples, prns, n_prns, interm_freq_hz, flags);
     });
 }

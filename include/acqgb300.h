@@ -137,7 +137,9 @@ int acq_plan_doppler_freqs(const acq_plan* plan, double* out);
  * `results` receives n_prns entries in the order of `prns`. When flags has
  * ACQ_FLAG_STORE_POWER_BINS, `power_bins` (host, may otherwise be NULL) receives
  * n_prns * num_doppler_bins * samples_per_code_eff float32, per PRN row-major
- * [doppler_row][code_col] (the transpose of Julia's column-major Matrix). Synchronous. */
+ * [doppler_row][code_col] (the transpose of Julia's column-major Matrix). Synchronous.
+ * n_prns = 0 (prns and results may be NULL) only checks the signal length, like acquire! with
+ * an empty PRN vector. */
 int acq_acquire(acq_plan* plan, const void* samples, int32_t dtype, int64_t n_samples,
                 const int32_t* prns, int32_t n_prns, double interm_freq_hz, uint32_t flags,
                 acq_result* results, float* power_bins);

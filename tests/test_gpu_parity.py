@@ -230,3 +230,15 @@ def test_tma_and_per_step_column_paths_agree(monkeypatch):
     for a, b in zip(ra, rb):
         assert (a.peak_doppler_bin, a.peak_code_bin) == (b.peak_doppler_bin, b.peak_code_bin)
         assert np.abs(a.power_bins - b.power_bins).max() <= 1e-5 * b.power_bins.max()
+
+
+def test_empty_prn_list_like_the_reference():
+    # acquire!(plan, signal, Int[]) checks the signal length and returns no results
+    # (src/acquire.jl:54-89)
+    plan = A.plan_acquire(A.GPSL1CA(), 4e6, [1, 2], num_noncoherent_accumulations=2)
+    x = np.zeros(2 * plan.samples_per_code, np.complex64)
+    assert A.acquire_b(plan, x, []) == []
+    assert A.acquire_b(plan, x, [], store_power_bins=True) == []
+    with pytest.raises(A.ArgumentError, match="Provide a longer signal"):
+        A.acquire_b(plan, x[: plan.samples_per_code], [])
+    assert len(A.acquire_b(plan, x, [2])) == 1
