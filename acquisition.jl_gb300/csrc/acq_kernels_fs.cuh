@@ -202,13 +202,16 @@ template <int N1, int N2>
 __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtensorMap tmap, ColTmaParams p) {
     constexpr int ND = N1 * N2;
     const int W = p.W, H = p.halo, AW = p.W + 2 * p.halo;
+    // each tile buffer starts on a 128-byte boundary (TMA destination): stride rounded up to
+    // 16 complex values
+    const int BS = (ND * W + 15) & ~15;
     extern __shared__ __align__(128) unsigned char smraw[];
     float2* buf[2];
     buf[0] = reinterpret_cast<float2*>(smraw);
-    buf[1] = buf[0] + ND * W;
-    float* accs = reinterpret_cast<float*>(buf[1] + ND * W);
+    buf[1] = buf[0] + BS;
+    float* accs = reinterpret_cast<float*>(buf[1] + BS);
     int* drs = reinterpret_cast<int*>(accs + ND * AW);
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(smraw) + ((2 * ND * W * 8 + ND * AW * 4 + p.n_nc * ND * 4 + 15) / 8);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smraw) + ((2 * BS * 8 + ND * AW * 4 + p.n_nc * ND * 4 + 15) / 8);
     const uint32_t tile_bytes = static_cast<uint32_t>(ND) * W * 8;
     if (threadIdx.x == 0) {
         mbar_init(&mbar[0], 1);

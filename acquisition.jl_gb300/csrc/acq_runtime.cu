@@ -388,11 +388,15 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
         code_drift_shifts(g, *P->sys, P->desc.sampling_freq_hz, m, dr.data());
         for (int v : dr) H = std::max(H, std::min(v, g.spc - v));
     }
-    if (H > W) return;
-    int box = 1;
+    if (H > W || W < 2 || W > 256 || W % 2) return;   // TMA: x * 8 B a multiple of 16 B, box <= 256
+    // rows per TMA box: the largest divisor of ndop up to 256 whose box keeps every box start in
+    // the shared tile on a 128-byte boundary (one box per tile always does)
+    int box = 0;
     for (int d = 1; d <= 256 && d <= g.ndop; ++d)
-        if (g.ndop % d == 0) box = d;
-    const size_t smem = 2 * sizeof(float2) * (size_t)g.ndop * W + sizeof(float) * (size_t)g.ndop * (W + 2 * H) +
+        if (g.ndop % d == 0 && (d == g.ndop || (static_cast<size_t>(d) * W * sizeof(float2)) % 128 == 0)) box = d;
+    if (box == 0) return;
+    const size_t tile_stride = (static_cast<size_t>(g.ndop) * W + 15) & ~static_cast<size_t>(15);
+    const size_t smem = 2 * sizeof(float2) * tile_stride + sizeof(float) * (size_t)g.ndop * (W + 2 * H) +
                         sizeof(int) * (size_t)g.n_nc * g.ndop + 16 + 16;
     if (smem > 200 * 1024) return;
     P->Tall.ensure(tall);
@@ -1417,7 +1421,8 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             CK(cudaStreamSynchronize(P->stream));
             int W = P->tmaW, cps = P->tmaCtasPerSm;
             if (option == ACQ_OPT_COLUMN_WIDTH) {
-                if (value != 8 && value != 16 && value != 32) throw AcqError(ACQ_ERR_ARGUMENT, "column width must be 8, 16 or 32");
+                if (value < 8 || value > 32 || value % 2)
+                    throw AcqError(ACQ_ERR_ARGUMENT, "column width must be even, in 8:32");
                 W = static_cast<int>(value);
             } else {
                 if (value < 1 || value > 32) throw AcqError(ACQ_ERR_ARGUMENT, "CTAs per SM must be in 1:32");

@@ -32,7 +32,8 @@ def test_shapes_give_the_same_results():
     ref = _run(plan, x)
     shapes = [{"tile_threads": 64, "tile_blocks": 3, "tile_pad": 1},
               {"tile_threads": 256, "tile_blocks": 20, "tile_pad": 0},
-              {"column_width": 8, "column_ctas_per_sm": 1}, {"column_width": 32}, {"form": "fused"}]
+              {"column_width": 8, "column_ctas_per_sm": 1}, {"column_width": 12}, {"column_width": 20},
+              {"column_width": 24, "column_ctas_per_sm": 2}, {"column_width": 32}, {"form": "fused"}]
     for sh in shapes:
         eff = T.apply(plan, sh)
         got = _run(plan, x)
@@ -43,6 +44,29 @@ def test_shapes_give_the_same_results():
         if "tile_threads" in sh:     # the tile stage does not reorder sums: identical
             assert all(np.array_equal(a[3], b[3]) for a, b in zip(ref, got)), sh
         T.apply(plan, start)
+
+
+def test_column_widths_with_several_tma_boxes():
+    # 500 Doppler bins: a tile is loaded as several boxes of rows (at most 256 each), and each box
+    # must start on a 128-byte boundary of the shared tile, which depends on the width
+    sats = [synth.Satellite(5, 45.0, 2100.0, 1234.5)]
+    plan = A.plan_acquire(A.GPSL1CA(), 12.5e6, [5, 6], min_doppler_coverage=16000,
+                          num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=2)
+    assert plan.num_doppler_bins == 500 and plan.geometry.fft_size == 500
+    x = synth.to_ci16(synth.synth(A.GPSL1CA(), 12.5e6, 270_000, sats, 8))
+    assert plan.get_option(6) == 16
+    start = T.current(plan)
+    ref = [(r.peak_doppler_bin, r.peak_code_bin, np.asarray(r.power_bins).copy())
+           for r in A.acquire_b(plan, x, [5, 6], store_power_bins=True)]
+    for w in (8, 12, 16):
+        assert plan.set_option(6, w) == w
+        got = A.acquire_b(plan, x, [5, 6], store_power_bins=True)
+        for a, r in zip(ref, got):
+            assert a[:2] == (r.peak_doppler_bin, r.peak_code_bin), w
+            assert np.abs(a[2] - np.asarray(r.power_bins)).max() <= 1e-6 * a[2].max(), w
+    # a width whose tiles exceed shared memory keeps the previous shape
+    assert plan.set_option(6, 32) == 16
+    T.apply(plan, start)
 
 
 def test_tune_applies_and_caches(tmp_path):
@@ -61,5 +85,7 @@ def test_option_validation():
     with pytest.raises(A.ArgumentError):
         plan.set_option(3, 48)          # tile threads not a multiple of 32
     with pytest.raises(A.ArgumentError):
-        plan.set_option(6, 12)          # column width
+        plan.set_option(6, 13)          # column width odd
+    with pytest.raises(A.ArgumentError):
+        plan.set_option(6, 34)          # column width above 32
     assert plan.get_option(0) in (0, 1)
