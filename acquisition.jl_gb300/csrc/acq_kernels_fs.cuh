@@ -15,11 +15,12 @@ namespace acq {
 // ------------------------------------------------------------------ specialised hot sizes
 // Coherent tile with the two-pass register FFT (F = N1 * N2): same mathematics as k_tile,
 // NF inverse FFTs per round; pass 1 forms S_g .* C*_m on the fly, pass 2 writes the first bs
-// lags of each row straight to the tile.
+// lags of each row straight to the tile. `twT` holds the pass-1 twiddles W_F^{n2 k1} at
+// [k1 * N2 + n2].
 template <int N1, int N2>
 __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, const float2* __restrict__ C,
                                                  const int* __restrict__ slots, int G, int nb, int bs, int spc,
-                                                 const float2* __restrict__ twF, int NF, float inv_F,
+                                                 const float2* __restrict__ twT, int NF, float inv_F,
                                                  float2* __restrict__ T, int64_t t_step_stride, int FS) {
     constexpr int F = N1 * N2;
     extern __shared__ float2 sm[];
@@ -50,7 +51,7 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
                 constexpr int k1 = decltype(kc)::value;
                 constexpr int pr = reg_perm(N1, k1);
                 float2 y = v[pr];
-                if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(twF, n2 * k1));
+                if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(twT, k1 * N2 + n2));
                 x[n2 + N2 * k1] = y;
             });
         }

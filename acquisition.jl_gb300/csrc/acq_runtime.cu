@@ -215,6 +215,7 @@ struct acq_plan {
     cudaStream_t stream = nullptr;
     FftDesc fftF{}, fftD{};
     DevBuf twF, twD;
+    DevBuf twT;   // pass-1 twiddles of the tile FFT, [k1][n2] = W_F^{n2 k1} (coalesced per k1)
     // plan-time constants
     DevBuf codes, conj, chips, pats, drift, sec, if_off;
     int64_t chips_len = 0;
@@ -475,6 +476,16 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         if (const char* e = std::getenv("ACQ_TILE_PAD")) P->tileFS = g.fft_size + std::atoi(e);
         P->smem_tile_fs = sizeof(float2) * (g.fft_size + (size_t)P->tileFS * P->tileNF);
         set_smem((const void*)P->tile_fs, P->smem_tile_fs);
+        // the same values as the F-point table at n2 * k1, laid out so that the threads of a warp
+        // (consecutive n2) read consecutive entries for each compile-time k1
+        std::vector<float2> h(static_cast<size_t>(g.fft_size));
+        for (int k1 = 0; k1 < n1; ++k1)
+            for (int q = 0; q < n2; ++q) {
+                const double a = -2.0 * M_PI * static_cast<double>(q * k1) / static_cast<double>(g.fft_size);
+                h[static_cast<size_t>(k1) * n2 + q] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
+            }
+        P->twT.ensure(sizeof(float2) * h.size());
+        CK(cudaMemcpy(P->twT.p, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice));
     }
     if (!getenv_flag("ACQ_GENERIC_FFT") && (g.ndop % 2) == 0) {
         if (g.path == 1) P->sign_fs = pick_sign_fs(g.ndop);
@@ -700,7 +711,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         const int nprn = static_cast<int>(P->prns.size());
         t_begin(P, ACQ_KERNEL_TILE);
         P->tile_fs<<<dim3(G, n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
-            P->S.as<float2>(), P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF,
+            P->S.as<float2>(), P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
             inv_F, P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
         t_end(P);
         ++L;
@@ -722,7 +733,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
             P->tile_fs<<<dim3(G, n), P->tileThreads, P->smem_tile_fs, st>>>(
-                Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->fftF.tw, P->tileNF, inv_F,
+                Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF, inv_F,
                 P->T.as<float2>(), 0, P->tileFS);
         else
             k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), a.d_slots, G, g.nb,
@@ -1132,7 +1143,7 @@ int acq_plan_destroy(acq_plan* P) {
     if (!P) return ACQ_OK;
     cudaSetDevice(P->device);
     if (P->stream) cudaStreamSynchronize(P->stream);
-    for (DevBuf* b : {&P->twF, &P->twD, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
+    for (DevBuf* b : {&P->twF, &P->twD, &P->twT, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
                       &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
                       &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted,
                       &P->dftB})
