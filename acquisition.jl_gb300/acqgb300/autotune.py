@@ -3,6 +3,7 @@
 Knobs (plan options of include/acqgb300.h). They move work between threads and CTAs; the tile
 knobs leave results bit-identical, the column and form knobs can change the order of the
 accumulation sums (results within FP32 rounding, decisions unchanged):
+  tile_rows            ACQ_OPT_TILE_ROWS           coherent-tile rows per CTA sharing each code-spectrum load
   tile_threads         ACQ_OPT_TILE_THREADS        threads per coherent-tile CTA
   tile_blocks          ACQ_OPT_TILE_BLOCKS         code blocks (inverse FFTs) per tile CTA round
   tile_pad             ACQ_OPT_TILE_PAD            shared-memory padding between FFT buffers
@@ -28,6 +29,7 @@ from typing import Callable
 from . import _lib as L
 
 KNOBS = {
+    "tile_rows": L.ACQ_OPT_TILE_ROWS,
     "tile_threads": L.ACQ_OPT_TILE_THREADS,
     "tile_blocks": L.ACQ_OPT_TILE_BLOCKS,
     "tile_pad": L.ACQ_OPT_TILE_PAD,
@@ -41,7 +43,7 @@ def candidates(plan) -> dict:
     """Candidate values per knob for this plan's geometry."""
     nb = plan.geometry.num_blocks
     blocks = sorted({b for b in (1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 25) if b <= nb})
-    return {"tile_threads": [64, 128, 192, 256], "tile_blocks": blocks, "tile_pad": [0, 1, 9],
+    return {"tile_rows": [1, 2], "tile_threads": [64, 128, 192, 256], "tile_blocks": blocks, "tile_pad": [0, 1, 9],
             "column_width": [8, 12, 16, 20, 24, 32], "column_ctas_per_sm": [1, 2, 3, 4, 6], "form": ["plain", "fused"]}
 
 

@@ -45,7 +45,8 @@ using RotMmaFn = void (*)(RotMmaParams);
 RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec, size_t* smem);
 
 
-TileFsFn pick_tile_fs(int fft_size);
+// coherent tile for an FFT size, transforming `rows` (1 or 2) rows per CTA
+TileFsFn pick_tile_fs(int fft_size, int rows);
 FusedFn pick_fused(int fft_size, int ndop);
 ColFsFn pick_col_fs(int ndop);
 ColTmaFn pick_col_tma(int ndop);

@@ -3,10 +3,13 @@
 
 namespace acq {
 
-#define ACQ_TILE_CASE(F) \
-    case F: return &k_tile_fs<best_split_n1(F), F / best_split_n1(F)>;
+#define ACQ_TILE_CASE(F)                                                                     \
+    case F:                                                                                  \
+        return rows == 2 ? &k_tile_fs<best_split_n1(F), F / best_split_n1(F), 2>             \
+                         : &k_tile_fs<best_split_n1(F), F / best_split_n1(F), 1>;
 
-TileFsFn pick_tile_fs(int F) {
+TileFsFn pick_tile_fs(int F, int rows) {
+    if (rows != 1 && rows != 2) return nullptr;
     switch (F) {
         ACQ_TILE_CASE(128) ACQ_TILE_CASE(256) ACQ_TILE_CASE(500) ACQ_TILE_CASE(1000) ACQ_TILE_CASE(1250)
         ACQ_TILE_CASE(1280) ACQ_TILE_CASE(1600) ACQ_TILE_CASE(2500)

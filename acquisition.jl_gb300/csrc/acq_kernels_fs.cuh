@@ -14,58 +14,76 @@ namespace acq {
 
 // ------------------------------------------------------------------ specialised hot sizes
 // Coherent tile with the two-pass register FFT (F = N1 * N2): same mathematics as k_tile,
-// NF inverse FFTs per round; pass 1 forms S_g .* C*_m on the fly, pass 2 writes the first bs
-// lags of each row straight to the tile. `twT` holds the pass-1 twiddles W_F^{n2 k1} at
-// [k1 * N2 + n2].
-template <int N1, int N2>
+// NF inverse FFTs per row and round; pass 1 forms S_g .* C*_m on the fly, pass 2 writes the
+// first bs lags of each row straight to the tile. `twT` holds the pass-1 twiddles W_F^{n2 k1} at
+// [k1 * N2 + n2]. A CTA transforms R rows g0, g0 + nb, ... that share g mod nb, so they use the
+// code blocks in the same order: each code-spectrum value loaded in pass 1 serves R products, and
+// each thread runs R independent FFTs. Every output value is computed by the same operations
+// whatever R is.
+template <int N1, int N2, int R>
 __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, const float2* __restrict__ C,
                                                  const int* __restrict__ slots, int G, int nb, int bs, int spc,
                                                  const float2* __restrict__ twT, int NF, float inv_F,
                                                  float2* __restrict__ T, int64_t t_step_stride, int FS) {
     constexpr int F = N1 * N2;
     extern __shared__ float2 sm[];
-    float2* sg = sm;
-    float2* buf = sm + F;   // nf buffers of stride FS >= F (padding staggers the banks of neighbouring FFTs)
-    const int g = blockIdx.x;
+    float2* sg = sm;            // R rows of S
+    float2* buf = sm + R * F;   // R * NF buffers of stride FS >= F (padding staggers the banks of neighbouring FFTs)
+    const int k = blockIdx.x % nb;
+    const int g0 = (blockIdx.x / nb) * R * nb + k;
+    const int nr = min(R, (G - g0 + nb - 1) / nb);   // rows of this CTA inside the plan's G
     const int pi = blockIdx.y;
     const int slot = slots[pi];
-    const int k = g % nb;
-    const float2* Sg = S + (static_cast<int64_t>(blockIdx.z) * G + g) * F;
-    for (int t = threadIdx.x; t < F; t += blockDim.x) sg[t] = Sg[t];
+#pragma unroll
+    for (int rho = 0; rho < R; ++rho) {
+        const float2* Sg = S + (static_cast<int64_t>(blockIdx.z) * G + g0 + rho * nb) * F;
+        for (int t = threadIdx.x; t < F; t += blockDim.x)
+            sg[rho * F + t] = rho < nr ? Sg[t] : make_float2(0.f, 0.f);
+    }
     __syncthreads();
-    float2* trow = T + blockIdx.z * t_step_stride + (static_cast<int64_t>(pi) * G + g) * spc;
+    float2* trow = T + blockIdx.z * t_step_stride + (static_cast<int64_t>(pi) * G + g0) * spc;
     for (int m0 = 0; m0 < nb; m0 += NF) {
         const int nf = min(NF, nb - m0);
         for (int task = threadIdx.x; task < nf * N2; task += blockDim.x) {
             const int f = task / N2, n2 = task - f * N2;
             const float2* Cm = C + (static_cast<int64_t>(slot) * nb + m0 + f) * F;
-            float2* x = buf + f * FS;
-            float2 v[N1];
+            float2 v[R][N1];
 #pragma unroll
             for (int n1 = 0; n1 < N1; ++n1) {
                 const int n = n2 + N2 * n1;
-                v[n1] = c_mul(sg[n], __ldg(Cm + n));
+                const float2 c = __ldg(Cm + n);
+#pragma unroll
+                for (int rho = 0; rho < R; ++rho) v[rho][n1] = c_mul(sg[rho * F + n], c);
             }
-            RegFFT<N1, true>::run(v);
+#pragma unroll
+            for (int rho = 0; rho < R; ++rho) RegFFT<N1, true>::run(v[rho]);
             static_for<0, N1>([&](auto kc) {
                 constexpr int k1 = decltype(kc)::value;
                 constexpr int pr = reg_perm(N1, k1);
-                float2 y = v[pr];
-                if (k1 != 0 && n2 != 0) y = c_mul(y, tw_load<true>(twT, k1 * N2 + n2));
-                x[n2 + N2 * k1] = y;
+                const bool twd = k1 != 0 && n2 != 0;
+                const float2 w = twd ? tw_load<true>(twT, k1 * N2 + n2) : make_float2(1.f, 0.f);
+#pragma unroll
+                for (int rho = 0; rho < R; ++rho) {
+                    float2 y = v[rho][pr];
+                    if (twd) y = c_mul(y, w);
+                    buf[(rho * NF + f) * FS + n2 + N2 * k1] = y;
+                }
             });
         }
         __syncthreads();
-        for (int task = threadIdx.x; task < nf * N1; task += blockDim.x) {
-            const int f = task / N1, k1 = task - f * N1;
-            const float2* x = buf + f * FS;
+        for (int task = threadIdx.x; task < R * nf * N1; task += blockDim.x) {
+            const int rho = task / (nf * N1);
+            const int rem = task - rho * nf * N1;
+            const int f = rem / N1, k1 = rem - f * N1;
+            if (rho >= nr) continue;
+            const float2* x = buf + (rho * NF + f) * FS;
             float2 v[N2];
 #pragma unroll
             for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[N2 * k1 + n2];
             RegFFT<N2, true>::run(v);
             int r = m0 + f - k;
             if (r < 0) r += nb;
-            float2* dst = trow + r * bs;
+            float2* dst = trow + static_cast<int64_t>(rho) * nb * spc + r * bs;
             static_for<0, N2>([&](auto kc) {
                 constexpr int k2 = decltype(kc)::value;
                 constexpr int pr = reg_perm(N2, k2);

@@ -227,7 +227,7 @@ struct acq_plan {
     // specialised two-pass FFT kernels for the plan's sizes (nullptr: generic kernels)
     TileFsFn tile_fs = nullptr;
     ColFsFn col_fs = nullptr;
-    int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1;
+    int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1, tileRows = 1;
     std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
     // data-bit / bit-edge stage split by sub-blocks
@@ -370,6 +370,17 @@ void setup_fused(acq_plan* P) {
     P->smem_fused = smem;
 }
 
+// Coherent-tile launch shape: shared memory (R rows of S, R * NF FFT buffers of stride FS) and
+// grid width (one CTA per group of R rows sharing g mod nb).
+size_t tile_smem(const acq_plan* P) {
+    return sizeof(float2) * static_cast<size_t>(P->tileRows) *
+           (P->g.fft_size + static_cast<size_t>(P->tileFS) * P->tileNF);
+}
+
+int tile_grid_x(const acq_plan* P) {
+    return P->g.nb * ((P->g.n_coh + P->tileRows - 1) / P->tileRows);
+}
+
 // TMA-staged column stage: T for all steps in HBM, a tensor map over it, a persistent grid.
 void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     const Geometry& g = P->g;
@@ -461,7 +472,7 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     set_smem((const void*)k_col_rot, P->smem_sign);
     upload_reg_twiddles();
     if (!getenv_flag("ACQ_GENERIC_FFT")) {
-        P->tile_fs = pick_tile_fs(g.fft_size);
+        P->tile_fs = pick_tile_fs(g.fft_size, 1);
         P->col_fs = g.path == 0 ? pick_col_fs(g.ndop) : nullptr;
     }
     if (P->tile_fs) {
@@ -474,7 +485,21 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         // stagger neighbouring FFT buffers by 9 float2 (18 banks) so warps spanning two FFTs don't conflict
         P->tileFS = g.fft_size + ((9 - (g.fft_size % 16) + 16) % 16);
         if (const char* e = std::getenv("ACQ_TILE_PAD")) P->tileFS = g.fft_size + std::atoi(e);
-        P->smem_tile_fs = sizeof(float2) * (g.fft_size + (size_t)P->tileFS * P->tileNF);
+        // two rows per CTA share the code-spectrum loads where the plan has rows to pair (the
+        // larger FFT sizes would need about twice the registers per thread for the second row)
+        int rows = (g.n_coh >= 2 && g.fft_size <= 1250) ? 2 : 1;
+        if (const char* e = std::getenv("ACQ_TILE_ROWS")) rows = std::atoi(e);
+        if (rows != 1) {
+            if (TileFsFn fn = pick_tile_fs(g.fft_size, rows)) {
+                P->tile_fs = fn;
+                P->tileRows = rows;
+                if (tile_smem(P) > 200 * 1024) {
+                    P->tile_fs = pick_tile_fs(g.fft_size, 1);
+                    P->tileRows = 1;
+                }
+            }
+        }
+        P->smem_tile_fs = tile_smem(P);
         set_smem((const void*)P->tile_fs, P->smem_tile_fs);
         // the same values as the F-point table at n2 * k1, laid out so that the threads of a warp
         // (consecutive n2) read consecutive entries for each compile-time k1
@@ -710,7 +735,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         // coherent tiles of every step in one launch, then the TMA-staged column stage
         const int nprn = static_cast<int>(P->prns.size());
         t_begin(P, ACQ_KERNEL_TILE);
-        P->tile_fs<<<dim3(G, n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
+        P->tile_fs<<<dim3(tile_grid_x(P), n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
             P->S.as<float2>(), P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
             inv_F, P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
         t_end(P);
@@ -732,7 +757,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_size;
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
-            P->tile_fs<<<dim3(G, n), P->tileThreads, P->smem_tile_fs, st>>>(
+            P->tile_fs<<<dim3(tile_grid_x(P), n), P->tileThreads, P->smem_tile_fs, st>>>(
                 Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF, inv_F,
                 P->T.as<float2>(), 0, P->tileFS);
         else
@@ -1367,6 +1392,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_TILE_THREADS: *value = P->tile_fs ? P->tileThreads : 0; break;
             case ACQ_OPT_TILE_BLOCKS: *value = P->tile_fs ? P->tileNF : 0; break;
             case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->g.fft_size : 0; break;
+            case ACQ_OPT_TILE_ROWS: *value = P->tile_fs ? P->tileRows : 0; break;
             case ACQ_OPT_COLUMN_WIDTH: *value = P->col_tma ? P->tmaW : 0; break;
             case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_tma ? P->tmaCtasPerSm : 0; break;
             default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
@@ -1397,30 +1423,47 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             if (effective) *effective = P->rot_prec;
             return;
         }
-        if (option == ACQ_OPT_TILE_THREADS || option == ACQ_OPT_TILE_BLOCKS || option == ACQ_OPT_TILE_PAD) {
+        if (option == ACQ_OPT_TILE_THREADS || option == ACQ_OPT_TILE_BLOCKS || option == ACQ_OPT_TILE_PAD ||
+            option == ACQ_OPT_TILE_ROWS) {
             const Geometry& g = P->g;
             if (!P->tile_fs) {
                 if (effective) *effective = 0;
                 return;
             }
             CK(cudaStreamSynchronize(P->stream));
+            const int old_threads = P->tileThreads, old_nf = P->tileNF, old_fs = P->tileFS, old_rows = P->tileRows;
+            TileFsFn old_fn = P->tile_fs;
             if (option == ACQ_OPT_TILE_THREADS) {
                 if (value < 32 || value > 256 || value % 32) throw AcqError(ACQ_ERR_ARGUMENT, "tile threads must be 32..256, a multiple of 32");
                 P->tileThreads = static_cast<int>(value);
             } else if (option == ACQ_OPT_TILE_BLOCKS) {
                 if (value < 1 || value > g.nb) throw AcqError(ACQ_ERR_ARGUMENT, "tile blocks per CTA must be in 1:num_blocks");
                 P->tileNF = static_cast<int>(value);
+            } else if (option == ACQ_OPT_TILE_ROWS) {
+                if (value != 1 && value != 2) throw AcqError(ACQ_ERR_ARGUMENT, "tile rows per CTA must be 1 or 2");
+                TileFsFn fn = pick_tile_fs(g.fft_size, static_cast<int>(value));
+                if (!fn) throw AcqError(ACQ_ERR_ARGUMENT, "no tile kernel for this FFT size");
+                P->tile_fs = fn;
+                P->tileRows = static_cast<int>(value);
             } else {
                 if (value < 0 || value > 32) throw AcqError(ACQ_ERR_ARGUMENT, "tile padding must be in 0:32");
                 P->tileFS = g.fft_size + static_cast<int>(value);
             }
-            const size_t smem = sizeof(float2) * (g.fft_size + (size_t)P->tileFS * P->tileNF);
-            if (smem > 200 * 1024) throw AcqError(ACQ_ERR_ARGUMENT, "tile configuration exceeds shared memory");
+            const size_t smem = tile_smem(P);
+            if (smem > 200 * 1024) {   // keep the previous shape
+                P->tileThreads = old_threads;
+                P->tileNF = old_nf;
+                P->tileFS = old_fs;
+                P->tileRows = old_rows;
+                P->tile_fs = old_fn;
+                throw AcqError(ACQ_ERR_ARGUMENT, "tile configuration exceeds shared memory");
+            }
             P->smem_tile_fs = smem;
             set_smem((const void*)P->tile_fs, P->smem_tile_fs);
             if (effective)
                 *effective = option == ACQ_OPT_TILE_THREADS ? P->tileThreads
                            : option == ACQ_OPT_TILE_BLOCKS  ? P->tileNF
+                           : option == ACQ_OPT_TILE_ROWS    ? P->tileRows
                                                             : P->tileFS - g.fft_size;
             return;
         }

@@ -655,7 +655,8 @@ def main():
     if not args.no_autotune:
         from acqgb300 import autotune as T
         tuned = T.tune(plan, dev, PRNS, reps=3, passes=1, store=False,
-                       knobs=("tile_threads", "tile_blocks", "tile_pad", "column_width", "column_ctas_per_sm"))
+                       knobs=("tile_rows", "tile_threads", "tile_blocks", "tile_pad", "column_width",
+                              "column_ctas_per_sm"))
 
     # warm-up (device-resident and public API)
     for _ in range(args.warmup):

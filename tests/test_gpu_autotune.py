@@ -11,6 +11,7 @@ from acqgb300 import synth
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
+L_TILE_ROWS = 9
 
 
 def _case():
@@ -32,6 +33,7 @@ def test_shapes_give_the_same_results():
     ref = _run(plan, x)
     shapes = [{"tile_threads": 64, "tile_blocks": 3, "tile_pad": 1},
               {"tile_threads": 256, "tile_blocks": 20, "tile_pad": 0},
+              {"tile_rows": 2}, {"tile_rows": 2, "tile_threads": 256, "tile_blocks": 4},
               {"column_width": 8, "column_ctas_per_sm": 1}, {"column_width": 12}, {"column_width": 20},
               {"column_width": 24, "column_ctas_per_sm": 2}, {"column_width": 32}, {"form": "fused"}]
     for sh in shapes:
@@ -41,9 +43,27 @@ def test_shapes_give_the_same_results():
         for a, b in zip(ref, got):
             assert a[:2] == b[:2], (sh, eff)
             assert np.abs(a[3] - b[3]).max() <= tol * a[3].max(), (sh, eff)
-        if "tile_threads" in sh:     # the tile stage does not reorder sums: identical
+        if "tile_threads" in sh or "tile_rows" in sh:     # the tile stage does not reorder sums: identical
             assert all(np.array_equal(a[3], b[3]) for a, b in zip(ref, got)), sh
         T.apply(plan, start)
+
+
+def test_two_tile_rows_per_cta_with_an_odd_row_count():
+    # 5 coherent periods: the last CTA of each code-block class holds one row, not two
+    sats = [synth.Satellite(7, 46.0, -1300.0, 321.75)]
+    plan = A.plan_acquire(A.GPSL1CA(), 5e6, [7, 8], min_doppler_coverage=5000,
+                          num_coherently_integrated_code_periods=5, num_noncoherent_accumulations=3)
+    assert plan.geometry.num_coherently_integrated_code_periods % 2 == 1
+    x = synth.to_ci16(synth.synth(A.GPSL1CA(), 5e6, 90_000, sats, 11))
+    if plan.get_option(L_TILE_ROWS) == 0:
+        pytest.skip("no specialised tile kernel for this FFT size")
+    ref = [np.asarray(r.power_bins).copy() for r in A.acquire_b(plan, x, [7, 8], store_power_bins=True)]
+    assert plan.set_option(L_TILE_ROWS, 2) == 2
+    got = [np.asarray(r.power_bins).copy() for r in A.acquire_b(plan, x, [7, 8], store_power_bins=True)]
+    assert all(np.array_equal(a, b) for a, b in zip(ref, got))
+    with pytest.raises(A.ArgumentError):
+        plan.set_option(L_TILE_ROWS, 3)
+    assert plan.get_option(L_TILE_ROWS) == 2
 
 
 def test_column_widths_with_several_tma_boxes():
