@@ -87,10 +87,14 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
             static_for<0, N2>([&](auto kc) {
                 constexpr int k2 = decltype(kc)::value;
                 constexpr int pr = reg_perm(N2, k2);
-                const int j = k1 + N1 * k2;
-                if (j < bs) {
-                    const float2 y = v[pr];
-                    dst[j] = make_float2(y.x * inv_F, y.y * inv_F);
+                // F >= 2 bs: lags from F / 2 on are never kept, so the FFT outputs feeding only
+                // them are dropped at compile time
+                if constexpr (N1 * k2 < F / 2) {
+                    const int j = k1 + N1 * k2;
+                    if (j < bs) {
+                        const float2 y = v[pr];
+                        dst[j] = make_float2(y.x * inv_F, y.y * inv_F);
+                    }
                 }
             });
         }
