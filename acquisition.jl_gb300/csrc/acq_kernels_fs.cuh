@@ -229,11 +229,11 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
     // 16 complex values
     const int BS = (ND * W + 15) & ~15;
     extern __shared__ __align__(128) unsigned char smraw[];
-    float2* buf[2];
-    buf[0] = reinterpret_cast<float2*>(smraw);
-    buf[1] = buf[0] + BS;
-    float* accs = reinterpret_cast<float*>(buf[1] + BS);
-    int* drs = reinterpret_cast<int*>(accs + ND * AW);
+    float2* const buf0 = reinterpret_cast<float2*>(smraw);   // buffer b at buf0 + b * BS
+    float* accs = reinterpret_cast<float*>(buf0 + 2 * BS);
+    // offs[m * ND + f]: shared-accumulator offset of FFT output f in step m (fftshifted row,
+    // row pitch, halo and that row's code drift), so pass 2 needs one load per output
+    int* offs = reinterpret_cast<int*>(accs + ND * AW);
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smraw) + ((2 * BS * 8 + ND * AW * 4 + p.n_nc * ND * 4 + 15) / 8);
     const uint32_t tile_bytes = static_cast<uint32_t>(ND) * W * 8;
     if (threadIdx.x == 0) {
@@ -241,10 +241,14 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
         mbar_init(&mbar[1], 1);
         mbar_fence_init();
     }
+    constexpr int half = ND / 2;
     for (int i = threadIdx.x; i < p.n_nc * ND; i += blockDim.x) {
-        int sh = p.drift[i];
+        const int m = i / ND, f = i - m * ND;
+        int row = f + half;
+        if (row >= ND) row -= ND;
+        int sh = p.drift[m * ND + row];
         if (sh > p.spc / 2) sh -= p.spc;
-        drs[i] = sh;
+        offs[i] = row * AW + H + sh;
     }
     for (int i = threadIdx.x; i < ND * AW; i += blockDim.x) accs[i] = 0.f;
     __syncthreads();
@@ -262,57 +266,61 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
         mbar_expect_tx(&mbar[b], tile_bytes);
         const int row0 = m * p.rows_per_step + pi * ND;
         for (int rb = 0; rb < p.n_boxes; ++rb)
-            tma_load_2d(buf[b] + rb * p.box_rows * W, &tmap, cb * W, row0 + rb * p.box_rows, &mbar[b]);
+            tma_load_2d(buf0 + b * BS + rb * p.box_rows * W, &tmap, cb * W, row0 + rb * p.box_rows, &mbar[b]);
     };
-    uint32_t phase[2] = {0u, 0u};
+    uint32_t phases = 0u;   // bit b: the parity to wait for on mbar[b]
+    // task -> (row of the pass, column) decompositions, stepped by blockDim.x without dividing by W
+    const int q0 = threadIdx.x / W, r0 = threadIdx.x - q0 * W;
+    const int dq = blockDim.x / W, dr = blockDim.x - dq * W;
     if (threadIdx.x == 0 && K > 0) issue(0);
-    constexpr int half = ND / 2;
     for (int k = 0; k < K; ++k) {
         const int b = k & 1;
         if (threadIdx.x == 0 && k + 1 < K) issue(k + 1);
-        if (!mbar_wait_bounded(&mbar[b], phase[b], p.err, 1)) {
+        if (!mbar_wait_bounded(&mbar[b], (phases >> b) & 1u, p.err, 1)) {
             // give the copies in flight a bounded chance to land, then leave
-            mbar_wait_bounded(&mbar[b ^ 1], phase[b ^ 1], p.err, 1);
+            mbar_wait_bounded(&mbar[b ^ 1], (phases >> (b ^ 1)) & 1u, p.err, 1);
             return;
         }
-        phase[b] ^= 1u;
+        phases ^= 1u << b;
         const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
         const int m = k % p.n_nc;
         const int pi = item / p.n_cblk, cb = item - pi * p.n_cblk;
         const int c0 = cb * W;
         const int wv = min(W, p.spc - c0);
-        float2* tl = buf[b];
-        for (int task = threadIdx.x; task < N2 * W; task += blockDim.x) {
-            const int n2 = task / W, t = task - n2 * W;
+        float2* tl = buf0 + b * BS;
+        for (int task = threadIdx.x, n2 = q0, t = r0; task < N2 * W;
+             task += blockDim.x, n2 += dq + (t + dr >= W), t += t + dr >= W ? dr - W : dr)
             fourstep_pass1<N1, N2, false>(tl + t, W, n2, p.twD);
-        }
         __syncthreads();
-        const int* dm = drs + m * ND;
-        for (int task = threadIdx.x; task < N1 * W; task += blockDim.x) {
-            const int k1 = task / W, t = task - k1 * W;
+        for (int task = threadIdx.x, k1 = q0, t = r0; task < N1 * W;
+             task += blockDim.x, k1 += dq + (t + dr >= W), t += t + dr >= W ? dr - W : dr) {
             if (t >= wv) continue;
             float2 v[N2];
 #pragma unroll
             for (int n2 = 0; n2 < N2; ++n2) v[n2] = tl[(N2 * k1 + n2) * W + t];
             RegFFT<N2, false>::run(v);
+            const int* om = offs + m * ND + k1;
+            float* at = accs + t;
             static_for<0, N2>([&](auto kc) {
                 constexpr int k2 = decltype(kc)::value;
                 constexpr int pr = reg_perm(N2, k2);
                 const float2 xv = v[pr];
                 const float pw = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
-                int row = k1 + N1 * k2 + half;
-                if (row >= ND) row -= ND;
-                float* cell = accs + row * AW + H + t + dm[row];
+                float* cell = at + om[N1 * k2];
                 *cell = __fadd_rn(*cell, pw);
             });
         }
         __syncthreads();
         if (m == p.n_nc - 1) {
             float* ap = p.acc + static_cast<int64_t>(pi) * ND * p.spc_eff;
+            // one half-warp (span <= 16) or warp per row: no division by the runtime span
             const int span = wv + 2 * H;
-            for (int i = threadIdx.x; i < ND * span; i += blockDim.x) {
-                const int row = i / span;
-                const int lc = -H + (i - row * span);
+            const int lpr = span <= 16 ? 16 : 32;
+            const int rstep = (blockDim.x / 32) * (32 / lpr);
+            const int lane = threadIdx.x & (lpr - 1);
+            for (int row = threadIdx.x / lpr; row < ND; row += rstep)
+            for (int j = lane; j < span; j += lpr) {
+                const int lc = j - H;
                 float* src = accs + row * AW + H + lc;
                 const float v = *src;
                 *src = 0.f;
