@@ -50,6 +50,8 @@ TileFsFn pick_tile_fs(int fft_size, int rows);
 FusedFn pick_fused(int fft_size, int ndop);
 ColFsFn pick_col_fs(int ndop);
 ColTmaFn pick_col_tma(int ndop);
+// TMA column stage that runs only the nb-point pass (the first pass applied by k_doppler_prepass)
+ColTmaFn pick_col_tma_pre(int nb);
 SignFsFn pick_sign_fs(int ndop);
 RotFsFn pick_rot_fs(int ndop);
 

@@ -6,13 +6,24 @@ namespace acq {
 #define ACQ_COL_CASE(N) \
     case N: return &k_col_simple_fs<best_split_n1(N), N / best_split_n1(N)>;
 #define ACQ_COLTMA_CASE(N) \
-    case N: return &k_col_tma<best_split_n1(N), N / best_split_n1(N)>;
+    case N: return &k_col_tma<best_split_n1(N), N / best_split_n1(N), false>;
+#define ACQ_COLTMA_PRE_CASE(N) \
+    case N: return &k_col_tma<1, N, true>;
 
 ColFsFn pick_col_fs(int ndop) {
     switch (ndop) {
         ACQ_COL_CASE(16) ACQ_COL_CASE(20) ACQ_COL_CASE(32) ACQ_COL_CASE(40) ACQ_COL_CASE(64) ACQ_COL_CASE(75)
         ACQ_COL_CASE(100) ACQ_COL_CASE(160) ACQ_COL_CASE(200) ACQ_COL_CASE(240) ACQ_COL_CASE(320) ACQ_COL_CASE(400)
         ACQ_COL_CASE(500) ACQ_COL_CASE(640) ACQ_COL_CASE(800) ACQ_COL_CASE(1280)
+        default: return nullptr;
+    }
+}
+
+ColTmaFn pick_col_tma_pre(int nb) {
+    switch (nb) {
+        ACQ_COLTMA_PRE_CASE(8) ACQ_COLTMA_PRE_CASE(10) ACQ_COLTMA_PRE_CASE(16) ACQ_COLTMA_PRE_CASE(20)
+        ACQ_COLTMA_PRE_CASE(25) ACQ_COLTMA_PRE_CASE(32) ACQ_COLTMA_PRE_CASE(40) ACQ_COLTMA_PRE_CASE(50)
+        ACQ_COLTMA_PRE_CASE(64)
         default: return nullptr;
     }
 }

@@ -208,6 +208,7 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 
 struct ColTmaParams {
     int spc, spc_eff, n_nc, W, halo, box_rows, n_boxes, n_items, n_cblk, rows_per_step;
+    int n1;                // pass-2 FFTs per column when the first pass was applied to the spectra
     const float2* twD;
     const int* drift;      // (n_nc, ndop) in [0, spc)
     float* acc;            // (n_req, ndop, spc_eff)
@@ -221,9 +222,16 @@ struct ColTmaParams {
 // into a shared accumulator with an H-column halo; it is written once per work item (interior
 // stored, halo/edge atomically added to the zeroed accumulator). Replaces the per-step column
 // kernel and its accumulator read-modify-write (src/noncoherent_integration.jl:482-592).
-template <int N1, int N2>
+//
+// PRE: the first four-step pass (N1 = n_coh points over the coherent periods q of the rows
+// k + nb q, times W_ndop^{k k1}) was applied to the signal spectra before the coherent tile
+// (k_doppler_prepass), which is linear in them and uses the same code blocks for all q of a
+// class k. The tile then holds row k + nb k1 = that pass's output, and this kernel runs only the
+// nb-point pass (N2 = nb, p.n1 = n_coh tasks per column).
+template <int N1, int N2, bool PRE>
 __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtensorMap tmap, ColTmaParams p) {
-    constexpr int ND = N1 * N2;
+    const int n1 = PRE ? p.n1 : N1;
+    const int ND = n1 * N2;
     const int W = p.W, H = p.halo, AW = p.W + 2 * p.halo;
     // each tile buffer starts on a 128-byte boundary (TMA destination): stride rounded up to
     // 16 complex values
@@ -241,7 +249,7 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
         mbar_init(&mbar[1], 1);
         mbar_fence_init();
     }
-    constexpr int half = ND / 2;
+    const int half = ND / 2;
     for (int i = threadIdx.x; i < p.n_nc * ND; i += blockDim.x) {
         const int m = i / ND, f = i - m * ND;
         int row = f + half;
@@ -288,11 +296,13 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
         const int c0 = cb * W;
         const int wv = min(W, p.spc - c0);
         float2* tl = buf0 + b * BS;
-        for (int task = threadIdx.x, n2 = q0, t = r0; task < N2 * W;
-             task += blockDim.x, n2 += dq + (t + dr >= W), t += t + dr >= W ? dr - W : dr)
-            fourstep_pass1<N1, N2, false>(tl + t, W, n2, p.twD);
-        __syncthreads();
-        for (int task = threadIdx.x, k1 = q0, t = r0; task < N1 * W;
+        if constexpr (!PRE) {
+            for (int task = threadIdx.x, n2 = q0, t = r0; task < N2 * W;
+                 task += blockDim.x, n2 += dq + (t + dr >= W), t += t + dr >= W ? dr - W : dr)
+                fourstep_pass1<N1, N2, false>(tl + t, W, n2, p.twD);
+            __syncthreads();
+        }
+        for (int task = threadIdx.x, k1 = q0, t = r0; task < n1 * W;
              task += blockDim.x, k1 += dq + (t + dr >= W), t += t + dr >= W ? dr - W : dr) {
             if (t >= wv) continue;
             float2 v[N2];
@@ -306,7 +316,7 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
                 constexpr int pr = reg_perm(N2, k2);
                 const float2 xv = v[pr];
                 const float pw = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
-                float* cell = at + om[N1 * k2];
+                float* cell = at + om[n1 * k2];
                 *cell = __fadd_rn(*cell, pw);
             });
         }

@@ -215,6 +215,7 @@ struct acq_plan {
     cudaStream_t stream = nullptr;
     FftDesc fftF{}, fftD{};
     DevBuf twF, twD;
+    DevBuf U;     // signal spectra after the first Doppler pass (PRE column mode), like S
     DevBuf twT;   // pass-1 twiddles of the tile FFT, [k1][n2] = W_F^{n2 k1} (coalesced per k1)
     // plan-time constants
     DevBuf codes, conj, chips, pats, drift, sec, if_off;
@@ -255,6 +256,7 @@ struct acq_plan {
     size_t smem_sfs = 0;
     // TMA-staged column stage over all steps (simple path)
     ColTmaFn col_tma = nullptr;
+    bool col_pre = false;   // col_tma runs only the nb-point pass; the tile reads U
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
     DevBuf chipperm, sorted;   // chip-sorted surface export (src/plot.jl:35-57)
@@ -370,6 +372,33 @@ void setup_fused(acq_plan* P) {
     P->smem_fused = smem;
 }
 
+// First pass of the Doppler four-step FFT applied to the signal block spectra (the PRE mode of
+// k_col_tma): for every step, code-block class k (< nb) and frequency bin nu,
+//   U[k + nb k1][nu] = W_ndop^{k k1} sum_q W_{n_coh}^{q k1} S[k + nb q][nu],   k1 < n_coh,
+// a direct n_coh-point DFT with the ndop-point table (W_{n_coh}^e = W_ndop^{e nb}).
+// The coherent tile is linear in S and uses the code block (k + r) mod nb for every row of class
+// k, so tiling U gives the first pass's output of the Doppler FFT of the tile of S.
+__global__ void __launch_bounds__(128) k_doppler_prepass(const float2* __restrict__ S, float2* __restrict__ U,
+                                                         int G, int nb, int n_coh, int F,
+                                                         const float2* __restrict__ twD) {
+    // one output per thread: nu from x, (k1, k) from y, step from z
+    const int nu = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nu >= F) return;
+    const int k1 = blockIdx.y / nb, k = blockIdx.y - k1 * nb;
+    const int64_t base = static_cast<int64_t>(blockIdx.z) * G;
+    float2 acc = S[(base + k) * F + nu];
+    int e = 0;   // (q k1) mod n_coh
+#pragma unroll 4
+    for (int q = 1; q < n_coh; ++q) {
+        e += k1;
+        if (e >= n_coh) e -= n_coh;
+        const float2 x = S[(base + k + nb * q) * F + nu];
+        acc = c_add(acc, e ? c_mul(x, __ldg(twD + e * nb)) : x);
+    }
+    if (k * k1) acc = c_mul(acc, __ldg(twD + k * k1));
+    U[(base + k + nb * k1) * F + nu] = acc;
+}
+
 // Coherent-tile launch shape: shared memory (R rows of S, R * NF FFT buffers of stride FS) and
 // grid width (one CTA per group of R rows sharing g mod nb).
 size_t tile_smem(const acq_plan* P) {
@@ -385,8 +414,15 @@ int tile_grid_x(const acq_plan* P) {
 void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     const Geometry& g = P->g;
     P->col_tma = nullptr;
+    P->col_pre = false;
     if (g.path != 0 || !P->tile_fs || getenv_flag("ACQ_GENERIC_FFT") || getenv_flag("ACQ_NO_TMA")) return;
     ColTmaFn fn = pick_col_tma(g.ndop);
+    bool pre = false;
+    if (g.n_coh <= 64 && !getenv_flag("ACQ_NO_PREPASS"))
+        if (ColTmaFn f2 = pick_col_tma_pre(g.nb)) {
+            fn = f2;
+            pre = true;
+        }
     if (!fn || (g.spc % 2) != 0) return;
     const size_t tall = sizeof(float2) * (size_t)g.n_nc * n_prns * g.ndop * g.spc;
     size_t cap = 4ull << 30;   // all-steps tile buffer per plan (batches hold many plans)
@@ -435,7 +471,9 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device));
     P->errflag.ensure(sizeof(int));
     CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
+    if (pre && g.n_coh > 1) P->U.ensure(sizeof(float2) * (size_t)g.n_nc * g.ndop * g.fft_size);
     P->col_tma = fn;
+    P->col_pre = pre;
     P->tmaW = W;
     P->tmaBoxRows = box;
     P->tmaBoxes = g.ndop / box;
@@ -734,9 +772,18 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     if (use_tma) {
         // coherent tiles of every step in one launch, then the TMA-staged column stage
         const int nprn = static_cast<int>(P->prns.size());
+        const float2* spectra = P->S.as<float2>();
+        if (P->col_pre && g.n_coh > 1) {   // one coherent period: the first pass is the identity
+            t_begin(P, ACQ_KERNEL_FRONTEND);
+            k_doppler_prepass<<<dim3((g.fft_size + 127) / 128, g.nb * g.n_coh, g.n_nc), 128, 0, st>>>(
+                P->S.as<float2>(), P->U.as<float2>(), G, g.nb, g.n_coh, g.fft_size, P->fftD.tw);
+            t_end(P);
+            ++L;
+            spectra = P->U.as<float2>();
+        }
         t_begin(P, ACQ_KERNEL_TILE);
         P->tile_fs<<<dim3(tile_grid_x(P), n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
-            P->S.as<float2>(), P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
+            spectra, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
             inv_F, P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
         t_end(P);
         ++L;
@@ -745,7 +792,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         ColTmaParams cp{};
         cp.spc = g.spc; cp.spc_eff = g.spc_eff; cp.n_nc = g.n_nc; cp.W = P->tmaW; cp.halo = P->tmaH;
         cp.box_rows = P->tmaBoxRows; cp.n_boxes = P->tmaBoxes; cp.n_cblk = (g.spc + P->tmaW - 1) / P->tmaW;
-        cp.n_items = n * cp.n_cblk; cp.rows_per_step = nprn * g.ndop;
+        cp.n_items = n * cp.n_cblk; cp.rows_per_step = nprn * g.ndop; cp.n1 = g.n_coh;
         cp.twD = P->fftD.tw; cp.drift = P->drift.as<int>(); cp.acc = P->accb.as<float>(); cp.err = P->errflag.as<int>();
         const int grid = std::max(1, std::min(P->tmaGrid, cp.n_items));
         t_begin(P, ACQ_KERNEL_COLUMN);
@@ -1168,7 +1215,7 @@ int acq_plan_destroy(acq_plan* P) {
     if (!P) return ACQ_OK;
     cudaSetDevice(P->device);
     if (P->stream) cudaStreamSynchronize(P->stream);
-    for (DevBuf* b : {&P->twF, &P->twD, &P->twT, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
+    for (DevBuf* b : {&P->twF, &P->twD, &P->twT, &P->U, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
                       &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
                       &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted,
                       &P->dftB})

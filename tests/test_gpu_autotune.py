@@ -66,6 +66,20 @@ def test_two_tile_rows_per_cta_with_an_odd_row_count():
     assert plan.get_option(L_TILE_ROWS) == 2
 
 
+def test_doppler_first_pass_on_the_spectra_matches_the_column_fft(monkeypatch):
+    # the first pass of the Doppler FFT (over the coherent periods) applied to the signal spectra
+    # before the coherent tile, against the full FFT in the column stage: same decisions, power
+    # surfaces within FP32 rounding
+    ref_plan, x = _case()
+    got = _run(ref_plan, x)
+    monkeypatch.setenv("ACQ_NO_PREPASS", "1")
+    plan, _ = _case()
+    ref = _run(plan, x)
+    for a, b in zip(ref, got):
+        assert a[:2] == b[:2]
+        assert np.abs(a[3] - b[3]).max() <= 1e-5 * a[3].max()
+
+
 def test_column_widths_with_several_tma_boxes():
     # 500 Doppler bins: a tile is loaded as several boxes of rows (at most 256 each), and each box
     # must start on a 128-byte boundary of the shared tile, which depends on the width
