@@ -14,8 +14,8 @@
 
 namespace acq {
 
-using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float,
-                          float2*, int64_t, int);
+using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float2*,
+                          int64_t, int);
 using FusedFn = void (*)(FusedParams);
 using ColFsFn = void (*)(const float2*, int, int, const float2*, const int*, int, int, float*, int);
 using ColTmaFn = void (*)(const CUtensorMap, ColTmaParams);

@@ -85,16 +85,20 @@ __global__ void k_code_spectra(const int8_t* __restrict__ codes, int spc, int nb
     float2* src = a;
     float2* dst = b;
     fft_block<false>(src, dst, fd, 1, F, 1, false);
+    // conjugated and scaled by 1/F, the inverse FFT's normalisation, so the tile kernels need no
+    // per-output scaling
     float2* out = C + static_cast<int64_t>(blockIdx.x) * F;
-    for (int t = threadIdx.x; t < F; t += blockDim.x) out[t] = make_float2(src[t].x, -src[t].y);
+    const float inv_F = 1.0f / static_cast<float>(F);
+    for (int t = threadIdx.x; t < F; t += blockDim.x) out[t] = make_float2(src[t].x * inv_F, -src[t].y * inv_F);
 }
 
 // ------------------------------------------------------------------ (a) coherent tile
 // Row g = p*nb + k, column block r of the coherent integration matrix:
-// (1/F) * IFFT(S_g .* C*_{(k+r) mod nb})[0:bs), src/coherent_integration.jl:136-171.
+// (1/F) * IFFT(S_g .* C*_{(k+r) mod nb})[0:bs), src/coherent_integration.jl:136-171 (the 1/F is
+// carried by the stored code spectra).
 // One CTA per (g, requested PRN); it reuses S_g for all nb code blocks, B IFFTs at a time.
 __global__ void k_tile(const float2* __restrict__ S, const float2* __restrict__ C, const int* __restrict__ slots,
-                       int G, int nb, int bs, int spc, FftDesc fd, int B, float inv_F, float2* __restrict__ T) {
+                       int G, int nb, int bs, int spc, FftDesc fd, int B, float2* __restrict__ T) {
     extern __shared__ float2 sm[];
     const int F = fd.n;
     float2* sg = sm;
@@ -125,7 +129,7 @@ __global__ void k_tile(const float2* __restrict__ S, const float2* __restrict__ 
             int r = m0 + bb - k;
             if (r < 0) r += nb;
             float2 v = src[bb * F + j];
-            trow[r * bs + j] = make_float2(v.x * inv_F, v.y * inv_F);
+            trow[r * bs + j] = v;
         }
         __syncthreads();
         if (src != A) {  // keep A as the product buffer for the next batch

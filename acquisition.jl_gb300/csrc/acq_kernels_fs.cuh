@@ -23,7 +23,7 @@ namespace acq {
 template <int N1, int N2, int R>
 __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, const float2* __restrict__ C,
                                                  const int* __restrict__ slots, int G, int nb, int bs, int spc,
-                                                 const float2* __restrict__ twT, int NF, float inv_F,
+                                                 const float2* __restrict__ twT, int NF,
                                                  float2* __restrict__ T, int64_t t_step_stride, int FS) {
     constexpr int F = N1 * N2;
     extern __shared__ float2 sm[];
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
                     const int j = k1 + N1 * k2;
                     if (j < bs) {
                         const float2 y = v[pr];
-                        dst[j] = make_float2(y.x * inv_F, y.y * inv_F);
+                        dst[j] = y;
                     }
                 }
             });
@@ -360,7 +360,6 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
 // Same mathematics as k_tile + k_col_simple_fs; the per-cell step order of the sums is kept.
 struct FusedParams {
     int G, nb, bs, spc, spc_eff, n_nc, rpc, cpc, nf, halo;
-    float inv_F;
     const float2* S;       // (n_nc, G, F)
     const float2* C;       // (slots, nb, F)
     const int* slots;
@@ -438,7 +437,7 @@ __global__ void __launch_bounds__(256) k_fused_simple(FusedParams fp) {
                         const int owner = j / CPC;
                         float2* dst = cluster.map_shared_rank(tile, owner);
                         const float2 y = v[pr];
-                        dst[g * CPC + (j - owner * CPC)] = make_float2(y.x * fp.inv_F, y.y * fp.inv_F);
+                        dst[g * CPC + (j - owner * CPC)] = y;
                     }
                 });
             }

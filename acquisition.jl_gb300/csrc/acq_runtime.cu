@@ -741,14 +741,13 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
                                                             use_if, if_step, a.d_if_off);
     t_end(P);
     ++L;
-    const float inv_F = 1.0f / static_cast<float>(g.fft_size);
     const bool use_fused = P->fused && P->form == ACQ_FORM_FUSED;
     if (use_fused) {
         if (P->fusedH > 0)
             CK(cudaMemsetAsync(P->accb.p, 0, sizeof(float) * (size_t)n * g.ndop * g.spc_eff, st));
         FusedParams fp{};
         fp.G = G; fp.nb = g.nb; fp.bs = g.bs; fp.spc = g.spc; fp.spc_eff = g.spc_eff; fp.n_nc = g.n_nc;
-        fp.rpc = P->fusedRPC; fp.cpc = P->fusedCPC; fp.nf = P->fusedNF; fp.halo = P->fusedH; fp.inv_F = inv_F;
+        fp.rpc = P->fusedRPC; fp.cpc = P->fusedCPC; fp.nf = P->fusedNF; fp.halo = P->fusedH;
         fp.S = P->S.as<float2>(); fp.C = P->conj.as<float2>(); fp.slots = a.d_slots;
         fp.twF = P->fftF.tw; fp.twD = P->fftD.tw; fp.drift = P->drift.as<int>(); fp.acc = P->accb.as<float>();
         cudaLaunchConfig_t cfg = {};
@@ -784,7 +783,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         t_begin(P, ACQ_KERNEL_TILE);
         P->tile_fs<<<dim3(tile_grid_x(P), n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
             spectra, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
-            inv_F, P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
+            P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
         t_end(P);
         ++L;
         if (P->tmaH > 0)
@@ -805,11 +804,11 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
             P->tile_fs<<<dim3(tile_grid_x(P), n), P->tileThreads, P->smem_tile_fs, st>>>(
-                Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF, inv_F,
+                Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
                 P->T.as<float2>(), 0, P->tileFS);
         else
             k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), a.d_slots, G, g.nb,
-                                                               g.bs, g.spc, P->fftF, P->tileB, inv_F, P->T.as<float2>());
+                                                               g.bs, g.spc, P->fftF, P->tileB, P->T.as<float2>());
         t_end(P);
         ++L;
         const int* dr = P->drift.as<int>() + (size_t)m * g.ndop;
