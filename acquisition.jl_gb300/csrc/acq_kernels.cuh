@@ -364,6 +364,9 @@ __global__ void k_stats(const float* __restrict__ acc, int ndop, int ncols, int 
                         unsigned long long* __restrict__ peakpart) {
     __shared__ float colred[8][kStatsCols];
     __shared__ unsigned long long keyred[8];
+    // per-lane FP32 row partials of a chunk of 32 rows; one thread per row sums its 32 partials
+    // in FP64 (instead of an FP64 shuffle tree run by every lane)
+    __shared__ float rowred[32][33];
     const int pi = blockIdx.y;
     const int nct = gridDim.x;
     const int c0 = blockIdx.x * kStatsCols;
@@ -374,30 +377,38 @@ __global__ void k_stats(const float* __restrict__ acc, int ndop, int ncols, int 
     for (int i = 0; i < kStatsCols / 32; ++i) cpart[i] = 0.f;
     unsigned long long best = 0ULL;
     double* rp = rowpart + (static_cast<int64_t>(pi) * nct + blockIdx.x) * ndop;
-    for (int e = wp; e < ndop; e += 8) {
-        float rs = 0.f;
-        const float* rowp = ap + static_cast<int64_t>(e) * ncols;
+    for (int e0 = 0; e0 < ndop; e0 += 32) {
+        // rows e0 + wp, e0 + wp + 8, ... of this chunk
+        for (int e = e0 + wp; e < min(e0 + 32, ndop); e += 8) {
+            float rs = 0.f;
+            const float* rowp = ap + static_cast<int64_t>(e) * ncols;
 #pragma unroll
-        for (int i = 0; i < kStatsCols / 32; ++i) {
-            const int c = c0 + lane + 32 * i;
-            if (c < ncols) {
-                const float v = rowp[c];
-                cpart[i] += v;
-                rs += v;
-                uint32_t order;
-                if (streamed_rot) {
-                    const int s = c / spc, cp = c - s * spc;
-                    order = (static_cast<uint32_t>(cp) * R + s) * static_cast<uint32_t>(ndop) + e;
-                } else {
-                    order = static_cast<uint32_t>(c) * ndop + e;
+            for (int i = 0; i < kStatsCols / 32; ++i) {
+                const int c = c0 + lane + 32 * i;
+                if (c < ncols) {
+                    const float v = rowp[c];
+                    cpart[i] += v;
+                    rs += v;
+                    uint32_t order;
+                    if (streamed_rot) {
+                        const int s = c / spc, cp = c - s * spc;
+                        order = (static_cast<uint32_t>(cp) * R + s) * static_cast<uint32_t>(ndop) + e;
+                    } else {
+                        order = static_cast<uint32_t>(c) * ndop + e;
+                    }
+                    const unsigned long long key = peak_key(v, order);
+                    best = key > best ? key : best;
                 }
-                const unsigned long long key = peak_key(v, order);
-                best = key > best ? key : best;
             }
+            rowred[e - e0][lane] = rs;
         }
-        double rsd = static_cast<double>(rs);
-        for (int o = 16; o > 0; o >>= 1) rsd += __shfl_xor_sync(0xffffffffu, rsd, o);
-        if (lane == 0) rp[e] = rsd;
+        __syncthreads();
+        if (threadIdx.x < 32 && e0 + static_cast<int>(threadIdx.x) < ndop) {
+            double rsd = 0.0;
+            for (int l = 0; l < 32; ++l) rsd += static_cast<double>(rowred[threadIdx.x][l]);
+            rp[e0 + threadIdx.x] = rsd;
+        }
+        __syncthreads();
     }
 #pragma unroll
     for (int i = 0; i < kStatsCols / 32; ++i) colred[wp][lane + 32 * i] = cpart[i];
