@@ -45,7 +45,11 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
     for (int m0 = 0; m0 < nb; m0 += NF) {
         const int nf = min(NF, nb - m0);
         for (int task = threadIdx.x; task < nf * N2; task += blockDim.x) {
-            const int f = task / N2, n2 = task - f * N2;
+            // odd FFTs of the round take n2 in descending order: a half-warp spanning FFTs f and
+            // f + 1 then reads one contiguous range of S positions (shared ones broadcast) instead
+            // of two ranges that fall on the same banks
+            const int f = task / N2, i = task - f * N2;
+            const int n2 = (f & 1) ? N2 - 1 - i : i;
             const float2* Cm = C + (static_cast<int64_t>(slot) * nb + m0 + f) * F;
             float2 v[R][N1];
 #pragma unroll
