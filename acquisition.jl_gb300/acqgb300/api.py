@@ -331,25 +331,38 @@ def _as_samples(signal):
     raise ArgumentError(f"unsupported signal dtype {a.dtype}")
 
 
+_RESULT_DTYPE = np.dtype([("prn", "<i4"), ("secondary_code_phase", "<i4"), ("carrier_doppler_hz", "<f8"),
+                          ("code_phase", "<f8"), ("cn0_dbhz", "<f8"), ("noise_power", "<f4"),
+                          ("peak_to_noise_ratio", "<f4"), ("peak_power", "<f4"),
+                          ("num_noncoherent_integrations", "<i4"), ("peak_doppler_bin", "<i4"),
+                          ("peak_code_bin", "<i4"), ("sign_pattern", "<i4"), ("bit_edge", "<i4"),
+                          ("detected", "<i4"), ("reserved", "<i4")])
+assert _RESULT_DTYPE.itemsize == C.sizeof(L.Result)
+
+
 def _results(plan: AcquisitionPlan, res_arr, prns, store_power_bins, bins):
+    """AcquisitionResults from the C result records (a ctypes array of Result, or a structured
+    numpy view of one; columns are pulled in bulk)."""
     g = plan.geometry
+    a = res_arr if isinstance(res_arr, np.ndarray) else np.frombuffer(res_arr, dtype=_RESULT_DTYPE, count=len(prns))
+    prn, sec = a["prn"].tolist(), a["secondary_code_phase"].tolist()
+    dop, cp, cn0 = a["carrier_doppler_hz"].tolist(), a["code_phase"].tolist(), a["cn0_dbhz"].tolist()
+    npow, pnr, ppow = a["noise_power"].copy(), a["peak_to_noise_ratio"].copy(), a["peak_power"].copy()
+    nnc, pdb, pcb = a["num_noncoherent_integrations"].tolist(), a["peak_doppler_bin"].tolist(), a["peak_code_bin"].tolist()
+    sgn, edge = a["sign_pattern"].tolist(), a["bit_edge"].tolist()
     out = []
-    for i, prn in enumerate(prns):
-        r = res_arr[i]
+    for i, p in enumerate(prns):
         pb = None
         if store_power_bins:
-            slot = plan.avail_prns.index(prn)
+            slot = plan.avail_prns.index(p)
             if plan.result_buffers[slot] is None:
                 plan.result_buffers[slot] = np.empty((g.num_doppler_bins, g.samples_per_code_eff), np.float32)
             np.copyto(plan.result_buffers[slot], bins[i])
             pb = plan.result_buffers[slot]
         out.append(AcquisitionResults(
-            plan.system, int(r.prn), plan.sampling_freq, float(r.carrier_doppler_hz), float(r.code_phase),
-            None if r.secondary_code_phase < 0 else int(r.secondary_code_phase), float(r.cn0_dbhz),
-            np.float32(r.noise_power), np.float32(r.peak_to_noise_ratio), int(r.num_noncoherent_integrations),
-            pb, plan.doppler_freqs, g.num_blocks, g.block_size, g.num_secondary_rotations,
-            np.float32(r.peak_power), int(r.peak_doppler_bin), int(r.peak_code_bin), int(r.sign_pattern),
-            int(r.bit_edge)))
+            plan.system, prn[i], plan.sampling_freq, dop[i], cp[i], None if sec[i] < 0 else sec[i], cn0[i],
+            npow[i], pnr[i], nnc[i], pb, plan.doppler_freqs, g.num_blocks, g.block_size,
+            g.num_secondary_rotations, ppow[i], pdb[i], pcb[i], sgn[i], edge[i]))
     return out
 
 

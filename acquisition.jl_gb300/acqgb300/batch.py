@@ -14,7 +14,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib as L
-from .api import (AcquisitionPlan, GNSSSystem, _as_samples, _check, _results, plan_acquire)
+from .api import (_RESULT_DTYPE, AcquisitionPlan, GNSSSystem, _as_samples, _check, _results, plan_acquire)
 
 class BatchItemC(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("dtype", C.c_int32), ("n_samples", C.c_int64),
@@ -92,10 +92,11 @@ class AcquisitionBatch:
     def fetch(self):
         res = (L.Result * self.total)()
         _check(_bind().acq_batch_fetch(self._h, res))
+        recs = np.frombuffer(res, dtype=_RESULT_DTYPE)
         out, k = [], 0
         for it in self.items:
             n = len(it.prns)
-            out.append(_results(it.plan, res[k:k + n], [int(p) for p in it.prns], False, None))
+            out.append(_results(it.plan, recs[k:k + n], [int(p) for p in it.prns], False, None))
             k += n
         return out
 

@@ -129,6 +129,29 @@ struct DevBuf {
     T* as() const { return static_cast<T*>(p); }
 };
 
+// Page-locked host staging (results and the error word), so fetches are asynchronous copies
+// followed by one stream synchronisation.
+struct PinnedBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void reset() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t n) {
+        if (n <= bytes) return;
+        reset();
+        if (n == 0) return;
+        cudaError_t e = cudaHostAlloc(&p, n, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw AcqError(ACQ_ERR_ALLOC, "cudaHostAlloc(" + std::to_string(n) + ") failed: " + cudaGetErrorString(e));
+        }
+        bytes = n;
+    }
+};
+
 FftDesc make_fft_desc(int n, DevBuf& tw) {
     FftDesc d{};
     d.n = n;
@@ -259,6 +282,7 @@ struct acq_plan {
     bool col_pre = false;   // col_tma runs only the nb-point pass; the tile reads U
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
+    PinnedBuf hstage;   // fetch staging: error word, then the results
     DevBuf chipperm, sorted;   // chip-sorted surface export (src/plot.jl:35-57)
     int tmaW = 16, tmaBoxRows = 1, tmaBoxes = 1, tmaGrid = 1, tmaH = 0, tmaCtasPerSm = 0;
     int n_plan_prns = 0;
@@ -1088,8 +1112,14 @@ void batch_free(acq_batch* B) {
 void fetch(acq_plan* P, acq_result* results, float* power_bins) {
     const Geometry& g = P->g;
     CK(cudaSetDevice(P->device));
-    if (results && P->last_n > 0)
-        CK(cudaMemcpyAsync(results, P->res.p, sizeof(acq_result) * P->last_n, cudaMemcpyDeviceToHost, P->stream));
+    // staging: [0, 8) the error word, [8, ...) the result records
+    const size_t res_bytes = (results && P->last_n > 0) ? sizeof(acq_result) * P->last_n : 0;
+    P->hstage.ensure(8 + res_bytes);
+    int* herr = static_cast<int*>(P->hstage.p);
+    acq_result* hres = reinterpret_cast<acq_result*>(static_cast<char*>(P->hstage.p) + 8);
+    *herr = 0;
+    if (P->errflag.p) CK(cudaMemcpyAsync(herr, P->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, P->stream));
+    if (res_bytes) CK(cudaMemcpyAsync(hres, P->res.p, res_bytes, cudaMemcpyDeviceToHost, P->stream));
     if (power_bins && P->last_n > 0 && (P->last_flags & ACQ_FLAG_STORE_POWER_BINS)) {
         const size_t cells = (size_t)P->last_n * g.ndop * g.spc_eff;
         const void* src = P->accb.p;
@@ -1105,9 +1135,9 @@ void fetch(acq_plan* P, acq_result* results, float* power_bins) {
     }
     CK(cudaStreamSynchronize(P->stream));
     t_collect(P);
+    if (res_bytes) std::memcpy(results, hres, res_bytes);
     if (P->errflag.p) {
-        int e = 0;
-        CK(cudaMemcpy(&e, P->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+        const int e = *herr;
         if (e != 0) {
             CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
             throw AcqError(ACQ_ERR_TIMEOUT, "a bounded wait for a TMA tile gave up (device error " +
@@ -1219,6 +1249,7 @@ int acq_plan_destroy(acq_plan* P) {
                       &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted,
                       &P->dftB})
         b->reset();
+    P->hstage.reset();
     for (cudaEvent_t e : P->ev_start) cudaEventDestroy(e);
     for (cudaEvent_t e : P->ev_stop) cudaEventDestroy(e);
     if (P->stream) cudaStreamDestroy(P->stream);
