@@ -275,6 +275,7 @@ Geometry compute_geometry(const acq_plan_desc& d) {
     g.nb = nb;
     g.bs = g.spc / nb;
     g.fft_size = nextprod_2357(2 * g.bs);
+    g.fft_tile = g.fft_size;
     g.ndb = (has_data && n_coh >= g.bit_period_codes) ? n_coh / g.bit_period_codes : 1;
     g.n_coh = n_coh;
     g.n_be = n_be;

@@ -36,6 +36,10 @@ const SystemInfo& system_info(int id);
 // Plan geometry, src/plan.jl:325-525.
 struct Geometry {
     int spc, spc_eff, nb, bs, fft_size, n_coh, ndb, n_be, n_nc, ndop, R, bit_period_codes;
+    // length of the block and coherent-tile transforms actually run: any length >= 2 bs gives the
+    // same lags 0..bs-1 of the linear correlation as fft_size (the reference's field, reported
+    // unchanged); the runtime may pick a faster one (see choose_fft_tile)
+    int fft_tile;
     int path;                 // 0 simple, 1 sign search, 2 rotation search
     double doppler_first, doppler_step, coverage;
     std::vector<double> doppler_freqs;

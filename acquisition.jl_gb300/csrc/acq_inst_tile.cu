@@ -11,8 +11,9 @@ namespace acq {
 TileFsFn pick_tile_fs(int F, int rows) {
     if (rows != 1 && rows != 2) return nullptr;
     switch (F) {
-        ACQ_TILE_CASE(128) ACQ_TILE_CASE(256) ACQ_TILE_CASE(500) ACQ_TILE_CASE(1000) ACQ_TILE_CASE(1250)
-        ACQ_TILE_CASE(1280) ACQ_TILE_CASE(1600) ACQ_TILE_CASE(2500)
+        ACQ_TILE_CASE(128) ACQ_TILE_CASE(256) ACQ_TILE_CASE(500) ACQ_TILE_CASE(512) ACQ_TILE_CASE(1000)
+        ACQ_TILE_CASE(1024) ACQ_TILE_CASE(1250) ACQ_TILE_CASE(1280) ACQ_TILE_CASE(1600) ACQ_TILE_CASE(2500)
+        ACQ_TILE_CASE(2560)
         default: return nullptr;
     }
 }
@@ -22,9 +23,10 @@ TileFsFn pick_tile_fs(int F, int rows) {
         return &k_fused_simple<best_split_n1(F), F / best_split_n1(F), best_split_n1(D), D / best_split_n1(D)>;
 
 FusedFn pick_fused(int fft, int ndop) {
-    ACQ_FUSED_CASE(500, 200) ACQ_FUSED_CASE(500, 16) ACQ_FUSED_CASE(500, 20) ACQ_FUSED_CASE(256, 16)
-    ACQ_FUSED_CASE(256, 32) ACQ_FUSED_CASE(128, 32) ACQ_FUSED_CASE(1280, 75) ACQ_FUSED_CASE(2500, 20)
-    ACQ_FUSED_CASE(1250, 320) ACQ_FUSED_CASE(1250, 16) ACQ_FUSED_CASE(500, 40) ACQ_FUSED_CASE(500, 400)
+    // transform lengths as chosen by the runtime (powers of two, or five times one, where possible)
+    ACQ_FUSED_CASE(512, 200) ACQ_FUSED_CASE(512, 16) ACQ_FUSED_CASE(512, 20) ACQ_FUSED_CASE(256, 16)
+    ACQ_FUSED_CASE(256, 32) ACQ_FUSED_CASE(128, 32) ACQ_FUSED_CASE(1280, 75) ACQ_FUSED_CASE(2560, 20)
+    ACQ_FUSED_CASE(1280, 320) ACQ_FUSED_CASE(1280, 16) ACQ_FUSED_CASE(512, 40) ACQ_FUSED_CASE(512, 400)
     return nullptr;
 }
 

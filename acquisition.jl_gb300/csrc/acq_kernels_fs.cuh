@@ -13,6 +13,8 @@
 namespace acq {
 
 // ------------------------------------------------------------------ specialised hot sizes
+__host__ __device__ constexpr int tile_row_pitch(int n2) { return n2 % 2 == 0 ? n2 + 1 : n2; }
+
 // Coherent tile with the two-pass register FFT (F = N1 * N2): same mathematics as k_tile,
 // NF inverse FFTs per row and round; pass 1 forms S_g .* C*_m on the fly, pass 2 writes the
 // first bs lags of each row straight to the tile. `twT` holds the pass-1 twiddles W_F^{n2 k1} at
@@ -26,9 +28,12 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
                                                  const float2* __restrict__ twT, int NF,
                                                  float2* __restrict__ T, int64_t t_step_stride, int FS) {
     constexpr int F = N1 * N2;
+    // row pitch of the pass-1 output in a buffer: pass-2 thread k1 reads row k1, so an even N2
+    // gets one element of padding (rows of a power-of-two length would share banks)
+    constexpr int P2 = tile_row_pitch(N2);
     extern __shared__ float2 sm[];
     float2* sg = sm;            // R rows of S
-    float2* buf = sm + R * F;   // R * NF buffers of stride FS >= F (padding staggers the banks of neighbouring FFTs)
+    float2* buf = sm + R * F;   // R * NF buffers of stride FS >= N1 * P2 (padding staggers the banks of neighbouring FFTs)
     const int k = blockIdx.x % nb;
     const int g0 = (blockIdx.x / nb) * R * nb + k;
     const int nr = min(R, (G - g0 + nb - 1) / nb);   // rows of this CTA inside the plan's G
@@ -70,7 +75,7 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
                 for (int rho = 0; rho < R; ++rho) {
                     float2 y = v[rho][pr];
                     if (twd) y = c_mul(y, w);
-                    buf[(rho * NF + f) * FS + n2 + N2 * k1] = y;
+                    buf[(rho * NF + f) * FS + n2 + P2 * k1] = y;
                 }
             });
         }
@@ -83,7 +88,7 @@ __global__ void __launch_bounds__(256) k_tile_fs(const float2* __restrict__ S, c
             const float2* x = buf + (rho * NF + f) * FS;
             float2 v[N2];
 #pragma unroll
-            for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[N2 * k1 + n2];
+            for (int n2 = 0; n2 < N2; ++n2) v[n2] = x[P2 * k1 + n2];
             RegFFT<N2, true>::run(v);
             int r = m0 + f - k;
             if (r < 0) r += nb;

@@ -252,6 +252,7 @@ struct acq_plan {
     TileFsFn tile_fs = nullptr;
     ColFsFn col_fs = nullptr;
     int tileNF = 1, Wfs = 1, tileThreads = 256, tileFS = 1, tileRows = 1;
+    int tileBase = 1;   // pass-1 buffer size before padding: N1 rows of pitch tile_row_pitch(N2)
     std::vector<int> step_has_drift;
     size_t smem_tile_fs = 0, smem_col_fs = 0;
     // data-bit / bit-edge stage split by sub-blocks
@@ -353,7 +354,7 @@ void setup_fused(acq_plan* P) {
     const Geometry& g = P->g;
     P->fused = nullptr;
     if (g.path != 0 || getenv_flag("ACQ_GENERIC_FFT")) return;
-    FusedFn fn = pick_fused(g.fft_size, g.ndop);
+    FusedFn fn = pick_fused(g.fft_tile, g.ndop);
     if (!fn) return;
     // signed drift bound over all steps (src/noncoherent_integration.jl:600-619)
     int H = 0;
@@ -367,7 +368,7 @@ void setup_fused(acq_plan* P) {
     const int cpc = (g.bs + CL - 1) / CL;
     if (H > cpc) return;
     const int nf = 8;   // one FFT buffer per warp
-    const size_t smem = sizeof(float2) * (size_t)g.ndop * cpc + sizeof(float2) * (size_t)nf * g.fft_size +
+    const size_t smem = sizeof(float2) * (size_t)g.ndop * cpc + sizeof(float2) * (size_t)nf * g.fft_tile +
                         sizeof(float) * (size_t)g.ndop * (cpc + 2 * H) + sizeof(int) * (size_t)g.ndop;
     if (smem > 220 * 1024) return;
     set_smem((const void*)fn, smem);
@@ -423,11 +424,28 @@ __global__ void __launch_bounds__(128) k_doppler_prepass(const float2* __restric
     U[(base + k + nb * k1) * F + nu] = acc;
 }
 
+// Transform length of the block FFTs and the coherent tile. Any length >= 2 bs gives the same lags
+// 0..bs-1 of the linear correlation (the circular wrap never reaches them), so a power of two, or
+// five times one, within 5 % above the reference's fft_size replaces it when a specialised tile
+// kernel exists: radix-4/8 stages are cheaper than radix-5/7 ones and the four-step split then
+// fills warps evenly. ACQ_REFERENCE_FFT_SIZE=1 keeps fft_size.
+int choose_fft_tile(const Geometry& g) {
+    if (getenv_flag("ACQ_REFERENCE_FFT_SIZE") || getenv_flag("ACQ_GENERIC_FFT")) return g.fft_size;
+    const int lo = 2 * g.bs;
+    for (int base : {1, 5}) {
+        long long L = base;
+        while (L < lo) L *= 2;
+        if (L == g.fft_size) return g.fft_size;
+        if (L * 100 <= 105LL * g.fft_size && pick_tile_fs(static_cast<int>(L), 1)) return static_cast<int>(L);
+    }
+    return g.fft_size;
+}
+
 // Coherent-tile launch shape: shared memory (R rows of S, R * NF FFT buffers of stride FS) and
 // grid width (one CTA per group of R rows sharing g mod nb).
 size_t tile_smem(const acq_plan* P) {
     return sizeof(float2) * static_cast<size_t>(P->tileRows) *
-           (P->g.fft_size + static_cast<size_t>(P->tileFS) * P->tileNF);
+           (P->g.fft_tile + static_cast<size_t>(P->tileFS) * P->tileNF);
 }
 
 int tile_grid_x(const acq_plan* P) {
@@ -495,7 +513,7 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device));
     P->errflag.ensure(sizeof(int));
     CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
-    if (pre && g.n_coh > 1) P->U.ensure(sizeof(float2) * (size_t)g.n_nc * g.ndop * g.fft_size);
+    if (pre && g.n_coh > 1) P->U.ensure(sizeof(float2) * (size_t)g.n_nc * g.ndop * g.fft_tile);
     P->col_tma = fn;
     P->col_pre = pre;
     P->tmaW = W;
@@ -511,14 +529,14 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     const Geometry& g = P->g;
     CK(cudaSetDevice(P->device));
     CK(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
-    P->fftF = make_fft_desc(g.fft_size, P->twF);
+    P->fftF = make_fft_desc(g.fft_tile, P->twF);
     P->fftD = make_fft_desc(g.ndop, P->twD);
     // launch shapes
-    P->smem_front = 2 * sizeof(float2) * g.fft_size;
+    P->smem_front = 2 * sizeof(float2) * g.fft_tile;
     if (P->smem_front > kSmemBudget)
-        throw AcqError(ACQ_ERR_UNSUPPORTED, "fft_size=" + std::to_string(g.fft_size) + " exceeds shared memory");
-    P->tileB = std::max(1, std::min(8, static_cast<int>((96 * 1024 / (sizeof(float2) * g.fft_size) - 1) / 2)));
-    P->smem_tile = sizeof(float2) * g.fft_size * (1 + 2 * P->tileB);
+        throw AcqError(ACQ_ERR_UNSUPPORTED, "fft_size=" + std::to_string(g.fft_tile) + " exceeds shared memory");
+    P->tileB = std::max(1, std::min(8, static_cast<int>((96 * 1024 / (sizeof(float2) * g.fft_tile) - 1) / 2)));
+    P->smem_tile = sizeof(float2) * g.fft_tile * (1 + 2 * P->tileB);
     P->Wsimple = std::max(1, std::min(32, pow2_floor(static_cast<int>(kSmemBudget / (16 * (size_t)g.ndop)))));
     if (16ull * g.ndop > kSmemBudget) throw AcqError(ACQ_ERR_UNSUPPORTED, "num_doppler_bins too large");
     P->smem_simple = 16ull * g.ndop * P->Wsimple;
@@ -534,29 +552,30 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     set_smem((const void*)k_col_rot, P->smem_sign);
     upload_reg_twiddles();
     if (!getenv_flag("ACQ_GENERIC_FFT")) {
-        P->tile_fs = pick_tile_fs(g.fft_size, 1);
+        P->tile_fs = pick_tile_fs(g.fft_tile, 1);
         P->col_fs = g.path == 0 ? pick_col_fs(g.ndop) : nullptr;
     }
     if (P->tile_fs) {
         // one round of pass-1 tasks per chunk: NF * N2 <= threads (N2 = fft_size / best_split_n1)
-        const int n1 = best_split_n1(g.fft_size), n2 = g.fft_size / std::max(1, n1);
+        const int n1 = best_split_n1(g.fft_tile), n2 = g.fft_tile / std::max(1, n1);
         P->tileThreads = 128;
         P->tileNF = std::max(1, std::min(g.nb, P->tileThreads / std::max(1, n2)));
         if (const char* e = std::getenv("ACQ_TILE_THREADS")) P->tileThreads = std::max(32, std::min(256, std::atoi(e)));
         if (const char* e = std::getenv("ACQ_TILE_NF")) P->tileNF = std::max(1, std::min(g.nb, std::atoi(e)));
         // stagger neighbouring FFT buffers by 9 float2 (18 banks) so warps spanning two FFTs don't conflict
-        P->tileFS = g.fft_size + ((9 - (g.fft_size % 16) + 16) % 16);
-        if (const char* e = std::getenv("ACQ_TILE_PAD")) P->tileFS = g.fft_size + std::atoi(e);
+        P->tileBase = n1 * tile_row_pitch(n2);
+        P->tileFS = P->tileBase + ((9 - (P->tileBase % 16) + 16) % 16);
+        if (const char* e = std::getenv("ACQ_TILE_PAD")) P->tileFS = P->tileBase + std::atoi(e);
         // two rows per CTA share the code-spectrum loads where the plan has rows to pair (the
         // larger FFT sizes would need about twice the registers per thread for the second row)
-        int rows = (g.n_coh >= 2 && g.fft_size <= 1250) ? 2 : 1;
+        int rows = (g.n_coh >= 2 && g.fft_tile <= 1250) ? 2 : 1;
         if (const char* e = std::getenv("ACQ_TILE_ROWS")) rows = std::atoi(e);
         if (rows != 1) {
-            if (TileFsFn fn = pick_tile_fs(g.fft_size, rows)) {
+            if (TileFsFn fn = pick_tile_fs(g.fft_tile, rows)) {
                 P->tile_fs = fn;
                 P->tileRows = rows;
                 if (tile_smem(P) > 200 * 1024) {
-                    P->tile_fs = pick_tile_fs(g.fft_size, 1);
+                    P->tile_fs = pick_tile_fs(g.fft_tile, 1);
                     P->tileRows = 1;
                 }
             }
@@ -565,10 +584,10 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         set_smem((const void*)P->tile_fs, P->smem_tile_fs);
         // the same values as the F-point table at n2 * k1, laid out so that the threads of a warp
         // (consecutive n2) read consecutive entries for each compile-time k1
-        std::vector<float2> h(static_cast<size_t>(g.fft_size));
+        std::vector<float2> h(static_cast<size_t>(g.fft_tile));
         for (int k1 = 0; k1 < n1; ++k1)
             for (int q = 0; q < n2; ++q) {
-                const double a = -2.0 * M_PI * static_cast<double>(q * k1) / static_cast<double>(g.fft_size);
+                const double a = -2.0 * M_PI * static_cast<double>(q * k1) / static_cast<double>(g.fft_tile);
                 h[static_cast<size_t>(k1) * n2 + q] = make_float2(static_cast<float>(std::cos(a)), static_cast<float>(std::sin(a)));
             }
         P->twT.ensure(sizeof(float2) * h.size());
@@ -650,7 +669,7 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         sample_codes_device(P->desc.system, P->chips.as<int8_t>(), P->chips_len, n_prns, g.spc,
                             P->desc.sampling_freq_hz, 0.0, 0.0, P->codes.as<int8_t>(), P->stream);
     }
-    P->conj.ensure(sizeof(float2) * (size_t)n_prns * g.nb * g.fft_size);
+    P->conj.ensure(sizeof(float2) * (size_t)n_prns * g.nb * g.fft_tile);
     k_code_spectra<<<n_prns * g.nb, kThreads, P->smem_front, P->stream>>>(P->codes.as<int8_t>(), g.spc, g.nb, g.bs,
                                                                            P->fftF, P->conj.as<float2>());
     CK(cudaGetLastError());
@@ -684,7 +703,7 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     CK(cudaMemcpy(P->drift.p, dr.data(), sizeof(int32_t) * dr.size(), cudaMemcpyHostToDevice));
     // per-acquisition buffers sized for all plan PRNs
     const size_t np = n_prns;
-    P->S.ensure(sizeof(float2) * (size_t)g.n_nc * g.ndop * g.fft_size);
+    P->S.ensure(sizeof(float2) * (size_t)g.n_nc * g.ndop * g.fft_tile);
     P->T.ensure(sizeof(float2) * np * g.ndop * g.spc);
     P->accb.ensure(sizeof(float) * np * g.ndop * g.spc_eff);
     if (g.path != 0) P->winb.ensure(sizeof(uint16_t) * np * g.ndop * g.spc_eff);
@@ -798,8 +817,8 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         const float2* spectra = P->S.as<float2>();
         if (P->col_pre && g.n_coh > 1) {   // one coherent period: the first pass is the identity
             t_begin(P, ACQ_KERNEL_FRONTEND);
-            k_doppler_prepass<<<dim3((g.fft_size + 127) / 128, g.nb * g.n_coh, g.n_nc), 128, 0, st>>>(
-                P->S.as<float2>(), P->U.as<float2>(), G, g.nb, g.n_coh, g.fft_size, P->fftD.tw);
+            k_doppler_prepass<<<dim3((g.fft_tile + 127) / 128, g.nb * g.n_coh, g.n_nc), 128, 0, st>>>(
+                P->S.as<float2>(), P->U.as<float2>(), G, g.nb, g.n_coh, g.fft_tile, P->fftD.tw);
             t_end(P);
             ++L;
             spectra = P->U.as<float2>();
@@ -824,7 +843,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         ++L;
     }
     for (int m = 0; m < ((use_fused || use_tma) ? 0 : g.n_nc); ++m) {
-        const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_size;
+        const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_tile;
         t_begin(P, ACQ_KERNEL_TILE);
         if (P->tile_fs)
             P->tile_fs<<<dim3(tile_grid_x(P), n), P->tileThreads, P->smem_tile_fs, st>>>(
@@ -1222,6 +1241,7 @@ int acq_plan_create(const acq_plan_desc* desc, const int32_t* prns, int32_t n_pr
         std::unique_ptr<acq_plan> P(new acq_plan());
         P->desc = *desc;
         P->g = compute_geometry(*desc);
+        P->g.fft_tile = choose_fft_tile(P->g);
         P->sys = &system_info(desc->system);
         for (int i = 0; i < n_prns; ++i) {
             if (prns[i] < 1 || prns[i] > P->sys->max_prn)
@@ -1468,7 +1488,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_MMA_SCALE_LOG2: *value = P->mma_scale_log2; break;
             case ACQ_OPT_TILE_THREADS: *value = P->tile_fs ? P->tileThreads : 0; break;
             case ACQ_OPT_TILE_BLOCKS: *value = P->tile_fs ? P->tileNF : 0; break;
-            case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->g.fft_size : 0; break;
+            case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->tileBase : 0; break;
             case ACQ_OPT_TILE_ROWS: *value = P->tile_fs ? P->tileRows : 0; break;
             case ACQ_OPT_COLUMN_WIDTH: *value = P->col_tma ? P->tmaW : 0; break;
             case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_tma ? P->tmaCtasPerSm : 0; break;
@@ -1518,13 +1538,13 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
                 P->tileNF = static_cast<int>(value);
             } else if (option == ACQ_OPT_TILE_ROWS) {
                 if (value != 1 && value != 2) throw AcqError(ACQ_ERR_ARGUMENT, "tile rows per CTA must be 1 or 2");
-                TileFsFn fn = pick_tile_fs(g.fft_size, static_cast<int>(value));
+                TileFsFn fn = pick_tile_fs(g.fft_tile, static_cast<int>(value));
                 if (!fn) throw AcqError(ACQ_ERR_ARGUMENT, "no tile kernel for this FFT size");
                 P->tile_fs = fn;
                 P->tileRows = static_cast<int>(value);
             } else {
                 if (value < 0 || value > 32) throw AcqError(ACQ_ERR_ARGUMENT, "tile padding must be in 0:32");
-                P->tileFS = g.fft_size + static_cast<int>(value);
+                P->tileFS = P->tileBase + static_cast<int>(value);
             }
             const size_t smem = tile_smem(P);
             if (smem > 200 * 1024) {   // keep the previous shape
@@ -1541,7 +1561,7 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
                 *effective = option == ACQ_OPT_TILE_THREADS ? P->tileThreads
                            : option == ACQ_OPT_TILE_BLOCKS  ? P->tileNF
                            : option == ACQ_OPT_TILE_ROWS    ? P->tileRows
-                                                            : P->tileFS - g.fft_size;
+                                                            : P->tileFS - P->tileBase;
             return;
         }
         if (option == ACQ_OPT_COLUMN_WIDTH || option == ACQ_OPT_COLUMN_CTAS_PER_SM) {
