@@ -523,6 +523,7 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->tmaCtasPerSm = ctas_per_sm > 0 ? std::min(per_sm, ctas_per_sm) : per_sm;
     P->tmaH = H;
     P->smem_col_tma = smem;
+
 }
 
 void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
@@ -737,6 +738,11 @@ void prepare_request(const acq_plan* P, int64_t n_samples, const int32_t* prns, 
     const Geometry& g = P->g;
     const int64_t seg_len = static_cast<int64_t>(g.n_coh) * g.spc;
     if (n <= 0) throw AcqError(ACQ_ERR_ARGUMENT, "no PRNs requested");
+    // the per-acquisition device buffers hold one surface per plan PRN; a request can repeat PRNs
+    // (each repeat is searched again, as in the reference) up to that count
+    if (n > static_cast<int>(P->prns.size()))
+        throw AcqError(ACQ_ERR_ARGUMENT, "a request may list at most " + std::to_string(P->prns.size()) +
+                                             " PRNs (the plan's PRN count), got " + std::to_string(n));
     slots.assign(n, 0);
     for (int i = 0; i < n; ++i) {
         auto it = std::find(P->prns.begin(), P->prns.end(), prns[i]);

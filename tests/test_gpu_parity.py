@@ -242,3 +242,16 @@ def test_empty_prn_list_like_the_reference():
     with pytest.raises(A.ArgumentError, match="Provide a longer signal"):
         A.acquire_b(plan, x[: plan.samples_per_code], [])
     assert len(A.acquire_b(plan, x, [2])) == 1
+
+
+def test_repeated_prns_up_to_the_plan_size():
+    # a repeated PRN is searched again and gives the same result; a request longer than the
+    # plan's PRN list is rejected (the device buffers hold one surface per plan PRN)
+    plan = A.plan_acquire(A.GPSL1CA(), 4e6, [1, 2, 3], num_noncoherent_accumulations=1)
+    rng = np.random.default_rng(5)
+    x = (rng.standard_normal(plan.samples_per_code) + 1j * rng.standard_normal(plan.samples_per_code)).astype(np.complex64)
+    a, b, c = A.acquire_b(plan, x, [2, 2, 1])
+    assert a.prn == b.prn == 2 and c.prn == 1
+    assert (a.peak_doppler_bin, a.peak_code_bin, a.noise_power) == (b.peak_doppler_bin, b.peak_code_bin, b.noise_power)
+    with pytest.raises(A.ArgumentError, match="at most 3 PRNs"):
+        A.acquire_b(plan, x, [1, 2, 3, 1])
