@@ -52,6 +52,8 @@ ColFsFn pick_col_fs(int ndop);
 ColTmaFn pick_col_tma(int ndop);
 // TMA column stage that runs only the nb-point pass (the first pass applied by k_doppler_prepass)
 ColTmaFn pick_col_tma_pre(int nb);
+// the same stage with work items per Doppler group k1 (tile = nb rows x W columns, 128 threads)
+ColTmaFn pick_col_tma_k1(int nb);
 SignFsFn pick_sign_fs(int ndop);
 RotFsFn pick_rot_fs(int ndop);
 

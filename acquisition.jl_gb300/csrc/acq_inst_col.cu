@@ -19,6 +19,21 @@ ColFsFn pick_col_fs(int ndop) {
     }
 }
 
+ColTmaFn pick_col_tma_k1(int nb) {
+    switch (nb) {
+        case 8: return &k_col_tma_k1<8>;
+        case 10: return &k_col_tma_k1<10>;
+        case 16: return &k_col_tma_k1<16>;
+        case 20: return &k_col_tma_k1<20>;
+        case 25: return &k_col_tma_k1<25>;
+        case 32: return &k_col_tma_k1<32>;
+        case 40: return &k_col_tma_k1<40>;
+        case 50: return &k_col_tma_k1<50>;
+        case 64: return &k_col_tma_k1<64>;
+        default: return nullptr;
+    }
+}
+
 ColTmaFn pick_col_tma_pre(int nb) {
     switch (nb) {
         ACQ_COLTMA_PRE_CASE(8) ACQ_COLTMA_PRE_CASE(10) ACQ_COLTMA_PRE_CASE(16) ACQ_COLTMA_PRE_CASE(20)

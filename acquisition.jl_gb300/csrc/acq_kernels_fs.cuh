@@ -355,6 +355,119 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
     }
 }
 
+// PRE-mode column stage by Doppler group: output (k1, k2) of a column needs only the nb tile rows
+// k1 * nb + k (k < nb), so a work item is (requested PRN, k1, block of W columns) and its tile is
+// nb rows x W columns: each row segment is W * 8 contiguous bytes (1 KB at W = 128) instead of the
+// narrow segments of all ndop rows. Per step: one TMA box into one of two shared buffers (the next
+// step's box loads while this one is transformed), one nb-point FFT per column, |X|^2 into a shared
+// accumulator of the item's nb output rows with an H-column halo (drift shift per row and step
+// from a per-item table), written once per item (interior stored, halo/edge atomically added to
+// the zeroed accumulator). Same mathematics as k_col_tma<1, nb, true>.
+template <int N2>
+__global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUtensorMap tmap, ColTmaParams p) {
+    const int n1 = p.n1, ND = n1 * N2, half = ND / 2;
+    const int W = p.W, H = p.halo, AW = W + 2 * H;
+    const int BS = (N2 * W + 15) & ~15;   // buffer stride (complex values), 128-byte aligned
+    extern __shared__ __align__(128) unsigned char smraw[];
+    float2* const buf0 = reinterpret_cast<float2*>(smraw);   // buffer b at buf0 + b * BS
+    float* accs = reinterpret_cast<float*>(buf0 + 2 * BS);   // N2 x AW
+    int* sht = reinterpret_cast<int*>(accs + N2 * AW);       // n_nc x N2: accumulator offset of output k2
+    int* rowof = sht + p.n_nc * N2;                          // N2: destination row of output k2
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smraw) + ((2 * BS * 8 + N2 * AW * 4 + (p.n_nc + 1) * N2 * 4 + 15) / 8);
+    const uint32_t tile_bytes = static_cast<uint32_t>(N2) * W * 8;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_fence_init();
+    }
+    for (int i = threadIdx.x; i < N2 * AW; i += blockDim.x) accs[i] = 0.f;
+    __syncthreads();
+    const int n_items = p.n_items;   // = n_req * n1 * n_cblk, item = (pi * n1 + k1) * n_cblk + cb
+    const int my_items = n_items > static_cast<int>(blockIdx.x)
+                             ? (n_items - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+                             : 0;
+    const int K = my_items * p.n_nc;
+    auto issue = [&](int k) {
+        const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
+        const int m = k % p.n_nc;
+        const int grp = item / p.n_cblk, cb = item - grp * p.n_cblk;   // grp = pi * n1 + k1
+        const int b = k & 1;
+        fence_proxy_async();
+        mbar_expect_tx(&mbar[b], tile_bytes);
+        tma_load_2d(buf0 + b * BS, &tmap, cb * W, m * p.rows_per_step + grp * N2, &mbar[b]);
+    };
+    uint32_t phases = 0u;   // bit b: the parity to wait for on mbar[b]
+    if (threadIdx.x == 0 && K > 0) issue(0);
+    for (int k = 0; k < K; ++k) {
+        const int b = k & 1;
+        const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
+        const int m = k % p.n_nc;
+        const int grp = item / p.n_cblk, cb = item - grp * p.n_cblk;
+        const int k1 = grp % n1, pi = grp / n1;
+        if (m == 0) {   // this item's output rows and per-step offsets (the epilogue synced before)
+            for (int i = threadIdx.x; i < (p.n_nc + 1) * N2; i += blockDim.x) {
+                const int mm = i / N2, k2 = i - mm * N2;
+                int row = k1 + n1 * k2 + half;
+                if (row >= ND) row -= ND;
+                if (mm == p.n_nc) {
+                    rowof[k2] = row;
+                } else {
+                    int sh = p.drift[mm * ND + row];
+                    if (sh > p.spc / 2) sh -= p.spc;
+                    sht[i] = k2 * AW + H + sh;
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0 && k + 1 < K) issue(k + 1);
+        if (!mbar_wait_bounded(&mbar[b], (phases >> b) & 1u, p.err, 1)) {
+            // give the copies in flight a bounded chance to land, then leave
+            mbar_wait_bounded(&mbar[b ^ 1], (phases >> (b ^ 1)) & 1u, p.err, 1);
+            return;
+        }
+        phases ^= 1u << b;
+        const int c0 = cb * W;
+        const int wv = min(W, p.spc - c0);
+        const float2* tl = buf0 + b * BS;
+        const int* om = sht + m * N2;
+        for (int t = threadIdx.x; t < wv; t += blockDim.x) {
+            float2 v[N2];
+#pragma unroll
+            for (int q = 0; q < N2; ++q) v[q] = tl[q * W + t];
+            RegFFT<N2, false>::run(v);
+            float* at = accs + t;
+            static_for<0, N2>([&](auto kc) {
+                constexpr int k2 = decltype(kc)::value;
+                constexpr int pr = reg_perm(N2, k2);
+                const float2 xv = v[pr];
+                const float pw = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
+                float* cell = at + om[k2];
+                *cell = __fadd_rn(*cell, pw);
+            });
+        }
+        __syncthreads();
+        if (m == p.n_nc - 1) {
+            float* ap = p.acc + static_cast<int64_t>(pi) * ND * p.spc_eff;
+            const int span = wv + 2 * H;
+            for (int k2 = threadIdx.x / 32; k2 < N2; k2 += blockDim.x / 32) {
+                float* arow = ap + static_cast<int64_t>(rowof[k2]) * p.spc_eff;
+                for (int j = threadIdx.x & 31; j < span; j += 32) {
+                    const int lc = j - H;
+                    float* src = accs + k2 * AW + H + lc;
+                    const float v = *src;
+                    *src = 0.f;
+                    int c = c0 + lc;
+                    if (c < 0) c += p.spc;
+                    if (c >= p.spc) c -= p.spc;
+                    if (H == 0 || (lc >= H && lc < wv - H)) arow[c] = v;
+                    else if (v != 0.f) atomicAdd(arow + c, v);
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // ------------------------------------------------------------------ fused simple path
 // One thread-block cluster of CL CTAs per (requested PRN, column block r) runs every
 // accumulation step of the simple path without touching HBM in between:

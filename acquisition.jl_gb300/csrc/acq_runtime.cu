@@ -281,6 +281,11 @@ struct acq_plan {
     // TMA-staged column stage over all steps (simple path)
     ColTmaFn col_tma = nullptr;
     bool col_pre = false;   // col_tma runs only the nb-point pass; the tile reads U
+    // PRE-mode column stage by Doppler group (used instead of col_tma when set)
+    ColTmaFn col_k1 = nullptr;
+    CUtensorMap tmapK1{};
+    int k1W = 128, k1Grid = 1, k1CtasPerSm = 0;
+    size_t smem_col_k1 = 0;
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
     PinnedBuf hstage;   // fetch staging: error word, then the results
@@ -452,11 +457,53 @@ int tile_grid_x(const acq_plan* P) {
     return P->g.nb * ((P->g.n_coh + P->tileRows - 1) / P->tileRows);
 }
 
+// PRE-mode column stage by Doppler group k1: tiles of nb rows x W columns of the all-steps tile
+// buffer (set up by setup_col_tma), 128 threads, a persistent grid. Leaves col_k1 null when the
+// shape does not fit.
+void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
+    const Geometry& g = P->g;
+    P->col_k1 = nullptr;
+    if (!P->col_tma || !P->col_pre || getenv_flag("ACQ_NO_COL_K1")) return;
+    ColTmaFn fn = pick_col_tma_k1(g.nb);
+    if (!fn || W < 2 || W > 256 || W % 2 || P->tmaH > W) return;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return;
+    const int H = P->tmaH;
+    const size_t bs = (static_cast<size_t>(g.nb) * W + 15) & ~static_cast<size_t>(15);
+    const size_t smem = 2 * sizeof(float2) * bs + sizeof(float) * (size_t)g.nb * (W + 2 * H) +
+                        sizeof(int) * (size_t)(g.n_nc + 1) * g.nb + 16 + 16;
+    if (smem > 200 * 1024) return;
+    cuuint64_t gdim[2] = {static_cast<cuuint64_t>(g.spc), static_cast<cuuint64_t>(g.n_nc) * n_prns * g.ndop};
+    cuuint64_t gstride[1] = {static_cast<cuuint64_t>(g.spc) * sizeof(float2)};
+    cuuint32_t bdim[2] = {static_cast<cuuint32_t>(W), static_cast<cuuint32_t>(g.nb)};
+    cuuint32_t estr[2] = {1, 1};
+    CUtensorMap map{};
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, P->Tall.p, gdim, gstride, bdim, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return;
+    set_smem((const void*)fn, smem);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, 128, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return;
+    }
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device));
+    P->tmapK1 = map;
+    P->col_k1 = fn;
+    P->k1W = W;
+    P->k1CtasPerSm = ctas_per_sm > 0 ? std::min(per_sm, ctas_per_sm) : per_sm;
+    P->k1Grid = sms * P->k1CtasPerSm;
+    P->smem_col_k1 = smem;
+}
+
 // TMA-staged column stage: T for all steps in HBM, a tensor map over it, a persistent grid.
 void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     const Geometry& g = P->g;
     P->col_tma = nullptr;
     P->col_pre = false;
+    P->col_k1 = nullptr;
     if (g.path != 0 || !P->tile_fs || getenv_flag("ACQ_GENERIC_FFT") || getenv_flag("ACQ_NO_TMA")) return;
     ColTmaFn fn = pick_col_tma(g.ndop);
     bool pre = false;
@@ -523,6 +570,7 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->tmaCtasPerSm = ctas_per_sm > 0 ? std::min(per_sm, ctas_per_sm) : per_sm;
     P->tmaH = H;
     P->smem_col_tma = smem;
+    if (pre) setup_col_k1(P, n_prns, P->k1W, P->k1CtasPerSm);
 
 }
 
@@ -842,9 +890,17 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         cp.box_rows = P->tmaBoxRows; cp.n_boxes = P->tmaBoxes; cp.n_cblk = (g.spc + P->tmaW - 1) / P->tmaW;
         cp.n_items = n * cp.n_cblk; cp.rows_per_step = nprn * g.ndop; cp.n1 = g.n_coh;
         cp.twD = P->fftD.tw; cp.drift = P->drift.as<int>(); cp.acc = P->accb.as<float>(); cp.err = P->errflag.as<int>();
-        const int grid = std::max(1, std::min(P->tmaGrid, cp.n_items));
         t_begin(P, ACQ_KERNEL_COLUMN);
-        P->col_tma<<<grid, kThreads, P->smem_col_tma, st>>>(P->tmapT, cp);
+        if (P->col_k1) {
+            cp.W = P->k1W;
+            cp.n_cblk = (g.spc + P->k1W - 1) / P->k1W;
+            cp.n_items = n * g.n_coh * cp.n_cblk;
+            const int grid = std::max(1, std::min(P->k1Grid, cp.n_items));
+            P->col_k1<<<grid, 128, P->smem_col_k1, st>>>(P->tmapK1, cp);
+        } else {
+            const int grid = std::max(1, std::min(P->tmaGrid, cp.n_items));
+            P->col_tma<<<grid, kThreads, P->smem_col_tma, st>>>(P->tmapT, cp);
+        }
         t_end(P);
         ++L;
     }
@@ -1496,8 +1552,8 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_TILE_BLOCKS: *value = P->tile_fs ? P->tileNF : 0; break;
             case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->tileBase : 0; break;
             case ACQ_OPT_TILE_ROWS: *value = P->tile_fs ? P->tileRows : 0; break;
-            case ACQ_OPT_COLUMN_WIDTH: *value = P->col_tma ? P->tmaW : 0; break;
-            case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_tma ? P->tmaCtasPerSm : 0; break;
+            case ACQ_OPT_COLUMN_WIDTH: *value = P->col_k1 ? P->k1W : P->col_tma ? P->tmaW : 0; break;
+            case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_k1 ? P->k1CtasPerSm : P->col_tma ? P->tmaCtasPerSm : 0; break;
             default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
         }
     });
@@ -1576,6 +1632,22 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
                 return;
             }
             CK(cudaStreamSynchronize(P->stream));
+            if (P->col_k1) {   // the Doppler-group form: tiles of nb rows x W columns
+                int W = P->k1W, cps = P->k1CtasPerSm;
+                if (option == ACQ_OPT_COLUMN_WIDTH) {
+                    if (value < 8 || value > 256 || value % 2)
+                        throw AcqError(ACQ_ERR_ARGUMENT, "column width must be even, in 8:256");
+                    W = static_cast<int>(value);
+                } else {
+                    if (value < 1 || value > 32) throw AcqError(ACQ_ERR_ARGUMENT, "CTAs per SM must be in 1:32");
+                    cps = static_cast<int>(value);
+                }
+                const int oldW = P->k1W, oldc = P->k1CtasPerSm;
+                setup_col_k1(P, P->n_plan_prns, W, cps);
+                if (!P->col_k1) setup_col_k1(P, P->n_plan_prns, oldW, oldc);   // keep the previous shape
+                if (effective) *effective = option == ACQ_OPT_COLUMN_WIDTH ? P->k1W : P->k1CtasPerSm;
+                return;
+            }
             int W = P->tmaW, cps = P->tmaCtasPerSm;
             if (option == ACQ_OPT_COLUMN_WIDTH) {
                 if (value < 8 || value > 32 || value % 2)

@@ -176,7 +176,8 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_OPT_TILE_THREADS 3       /* coherent-tile kernel: threads per CTA (32..256, multiple of 32) */
 #define ACQ_OPT_TILE_BLOCKS 4        /*   code blocks (inverse FFTs) per CTA round (1..num_blocks) */
 #define ACQ_OPT_TILE_PAD 5           /*   shared-memory padding between FFT buffers, complex elements (0..32) */
-#define ACQ_OPT_COLUMN_WIDTH 6       /* TMA column kernel: code-phase columns per tile (even, 8..32) */
+#define ACQ_OPT_COLUMN_WIDTH 6       /* TMA column kernel: code-phase columns per tile (even; 8..32, or 8..256
+                                        for the Doppler-group form of the simple path) */
 #define ACQ_OPT_COLUMN_CTAS_PER_SM 7 /*   persistent CTAs per SM (1..occupancy limit) */
 #define ACQ_OPT_DOPPLER_PRECISION 8  /* simple path: the per-column Doppler DFT as a dense DFT-matrix GEMM on the
                                         tensor cores (ACQ_PREC_*; ndop <= 250), or FP32 FFTs (default) */

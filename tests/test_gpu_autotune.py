@@ -80,9 +80,31 @@ def test_doppler_first_pass_on_the_spectra_matches_the_column_fft(monkeypatch):
         assert np.abs(a[3] - b[3]).max() <= 1e-5 * a[3].max()
 
 
-def test_column_widths_with_several_tma_boxes():
+def test_doppler_group_column_stage_matches_the_full_tile_form(monkeypatch):
+    # tiles of one Doppler group (nb rows x W columns) against tiles of all ndop rows: the same
+    # sums per cell in the same step order, so the same decisions and surfaces within rounding
+    plan, x = _case()
+    got = _run(plan, x)
+    assert plan.get_option(6) >= 8
+    monkeypatch.setenv("ACQ_NO_COL_K1", "1")
+    ref_plan, _ = _case()
+    ref = _run(ref_plan, x)
+    monkeypatch.delenv("ACQ_NO_COL_K1")   # read again whenever a plan's column shape is set up
+    for a, b in zip(ref, got):
+        assert a[:2] == b[:2]
+        assert np.abs(a[3] - b[3]).max() <= 1e-6 * a[3].max()
+    for w in (32, 64, 256):
+        assert plan.set_option(6, w) == w
+        for a, b in zip(ref, _run(plan, x)):
+            assert a[:2] == b[:2], w
+            assert np.abs(a[3] - b[3]).max() <= 1e-6 * a[3].max(), w
+
+
+def test_column_widths_with_several_tma_boxes(monkeypatch):
     # 500 Doppler bins: a tile is loaded as several boxes of rows (at most 256 each), and each box
-    # must start on a 128-byte boundary of the shared tile, which depends on the width
+    # must start on a 128-byte boundary of the shared tile, which depends on the width (the full
+    # column FFT, without the first pass on the spectra)
+    monkeypatch.setenv("ACQ_NO_PREPASS", "1")
     sats = [synth.Satellite(5, 45.0, 2100.0, 1234.5)]
     plan = A.plan_acquire(A.GPSL1CA(), 12.5e6, [5, 6], min_doppler_coverage=16000,
                           num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=2)
@@ -121,5 +143,5 @@ def test_option_validation():
     with pytest.raises(A.ArgumentError):
         plan.set_option(6, 13)          # column width odd
     with pytest.raises(A.ArgumentError):
-        plan.set_option(6, 34)          # column width above 32
+        plan.set_option(6, 258)         # column width above 256
     assert plan.get_option(0) in (0, 1)
