@@ -106,6 +106,26 @@ __global__ void k_gather_cols(const float* __restrict__ in, int64_t rows, int64_
     }
 }
 
+// Zeroes the accumulator cells that the TMA column stages add to atomically: the columns within
+// H of a column-block boundary (multiples of W, and spc, wrapping to 0). Every other cell is
+// stored by exactly one work item, so the accumulator needs no full clear.
+__global__ void k_zero_edges(float* __restrict__ acc, int64_t rows, int spc, int spc_eff, int W, int H,
+                             int n_bound) {
+    const int per_row = n_bound * 2 * H;
+    const int64_t total = rows * per_row;
+    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < total;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = k / per_row;
+        const int e = static_cast<int>(k - r * per_row);
+        const int j = e / (2 * H), o = e - j * 2 * H - H;   // boundary j, offset in [-H, H)
+        const int b = j == n_bound - 1 ? spc : j * W;
+        int c = b + o;
+        if (c < 0) c += spc;
+        if (c >= spc) c -= spc;
+        acc[r * spc_eff + c] = 0.f;
+    }
+}
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -289,6 +309,12 @@ struct acq_plan {
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
     PinnedBuf hstage;   // fetch staging: error word, then the results
+    // request metadata (slots, PRN ids, IF offsets) staged in page-locked memory for one
+    // asynchronous copy; two buffers, each reused only after its previous copy has run
+    PinnedBuf hreq[2];
+    cudaEvent_t hreq_ev[2] = {nullptr, nullptr};
+    int hreq_next = 0;
+    DevBuf dreq;
     DevBuf chipperm, sorted;   // chip-sorted surface export (src/plot.jl:35-57)
     int tmaW = 16, tmaBoxRows = 1, tmaBoxes = 1, tmaGrid = 1, tmaH = 0, tmaCtasPerSm = 0;
     int n_plan_prns = 0;
@@ -883,8 +909,15 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
         t_end(P);
         ++L;
-        if (P->tmaH > 0)
-            CK(cudaMemsetAsync(P->accb.p, 0, sizeof(float) * (size_t)n * g.ndop * g.spc_eff, st));
+        if (P->tmaH > 0) {
+            const int wc = P->col_k1 ? P->k1W : P->tmaW;
+            const int n_bound = (g.spc + wc - 1) / wc + 1;
+            const int64_t rows = static_cast<int64_t>(n) * g.ndop;
+            const int64_t total = rows * n_bound * 2 * P->tmaH;
+            k_zero_edges<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
+                P->accb.as<float>(), rows, g.spc, g.spc_eff, wc, P->tmaH, n_bound);
+            ++L;
+        }
         ColTmaParams cp{};
         cp.spc = g.spc; cp.spc_eff = g.spc_eff; cp.n_nc = g.n_nc; cp.W = P->tmaW; cp.halo = P->tmaH;
         cp.box_rows = P->tmaBoxRows; cp.n_boxes = P->tmaBoxes; cp.n_cblk = (g.spc + P->tmaW - 1) / P->tmaW;
@@ -1038,13 +1071,25 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
     prepare_request(P, n_samples, prns, n, interm_freq, slots, offs, a.use_if, a.if_step);
     CK(cudaSetDevice(P->device));
     cudaStream_t st = P->stream;
-    CK(cudaMemcpyAsync(P->slots.p, slots.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(P->prn_ids.p, prns, sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    if (a.use_if) CK(cudaMemcpyAsync(P->if_off.p, offs.data(), sizeof(float) * offs.size(), cudaMemcpyHostToDevice, st));
+    // [slots (n) | PRN ids (n) | IF offsets (n_nc)] in one copy from page-locked memory
+    const size_t bytes = sizeof(int) * 2 * static_cast<size_t>(n) + sizeof(float) * offs.size();
+    const int hb = P->hreq_next;
+    P->hreq_next ^= 1;
+    if (P->hreq_ev[hb]) CK(cudaEventSynchronize(P->hreq_ev[hb]));
+    else CK(cudaEventCreateWithFlags(&P->hreq_ev[hb], cudaEventDisableTiming));
+    P->hreq[hb].ensure(bytes);
+    P->dreq.ensure(bytes);
+    char* h = static_cast<char*>(P->hreq[hb].p);
+    std::memcpy(h, slots.data(), sizeof(int) * n);
+    std::memcpy(h + sizeof(int) * n, prns, sizeof(int) * n);
+    if (!offs.empty()) std::memcpy(h + sizeof(int) * 2 * n, offs.data(), sizeof(float) * offs.size());
+    CK(cudaMemcpyAsync(P->dreq.p, h, bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaEventRecord(P->hreq_ev[hb], st));
     a.n = n;
-    a.d_slots = P->slots.as<int>();
-    a.d_prn_ids = P->prn_ids.as<int>();
-    a.d_if_off = P->if_off.as<float>();
+    char* d = P->dreq.as<char>();
+    a.d_slots = reinterpret_cast<const int*>(d);
+    a.d_prn_ids = reinterpret_cast<const int*>(d + sizeof(int) * n);
+    a.d_if_off = reinterpret_cast<const float*>(d + sizeof(int) * 2 * n);
     a.interm_freq = interm_freq;
     a.flags = flags;
     a.d_res = P->res.as<acq_result>();
@@ -1329,9 +1374,13 @@ int acq_plan_destroy(acq_plan* P) {
     for (DevBuf* b : {&P->twF, &P->twD, &P->twT, &P->U, &P->codes, &P->conj, &P->chips, &P->pats, &P->drift, &P->sec, &P->if_off,
                       &P->input, &P->S, &P->T, &P->accb, &P->winb, &P->rowpart, &P->colsum, &P->peakpart, &P->zs,
                       &P->res, &P->slots, &P->prn_ids, &P->Tall, &P->errflag, &P->chipperm, &P->sorted,
-                      &P->dftB})
+                      &P->dftB, &P->dreq})
         b->reset();
     P->hstage.reset();
+    for (int i = 0; i < 2; ++i) {
+        P->hreq[i].reset();
+        if (P->hreq_ev[i]) cudaEventDestroy(P->hreq_ev[i]);
+    }
     for (cudaEvent_t e : P->ev_start) cudaEventDestroy(e);
     for (cudaEvent_t e : P->ev_stop) cudaEventDestroy(e);
     if (P->stream) cudaStreamDestroy(P->stream);
