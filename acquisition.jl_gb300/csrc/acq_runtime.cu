@@ -313,6 +313,25 @@ struct acq_plan {
     // asynchronous copy; two buffers, each reused only after its previous copy has run
     PinnedBuf hreq[2];
     cudaEvent_t hreq_ev[2] = {nullptr, nullptr};
+    // the launch sequence of a repeated request, replayed as one CUDA graph (captured on the second
+    // identical request in a row; `version` changes with every plan option)
+    struct RequestKey {
+        const void* d_in = nullptr;
+        const void* dreq = nullptr;
+        int dtype = -1, n = -1, use_if = 0;
+        uint32_t flags = 0;
+        float if_step = 0.f;
+        double interm = 0.0;
+        uint64_t version = 0;
+        bool operator==(const RequestKey& o) const {
+            return d_in == o.d_in && dreq == o.dreq && dtype == o.dtype && n == o.n && use_if == o.use_if &&
+                   flags == o.flags && if_step == o.if_step && interm == o.interm && version == o.version;
+        }
+    };
+    RequestKey last_key, graph_key;
+    cudaGraphExec_t gexec = nullptr;
+    int64_t graph_launches = 0;
+    uint64_t version = 1;
     int hreq_next = 0;
     DevBuf dreq;
     DevBuf chipperm, sorted;   // chip-sorted surface export (src/plot.jl:35-57)
@@ -1093,7 +1112,45 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
     a.interm_freq = interm_freq;
     a.flags = flags;
     a.d_res = P->res.as<acq_result>();
-    P->launches = launch_sequence(P, st, d_in, dtype, a);
+    acq_plan::RequestKey key;
+    key.d_in = d_in; key.dreq = P->dreq.p; key.dtype = dtype; key.n = n; key.use_if = a.use_if; key.flags = flags;
+    key.if_step = a.if_step; key.interm = interm_freq; key.version = P->version;
+    if (P->timing || getenv_flag("ACQ_NO_GRAPH")) {
+        P->launches = launch_sequence(P, st, d_in, dtype, a);
+    } else if (P->gexec && key == P->graph_key) {
+        CK(cudaGraphLaunch(P->gexec, st));
+        P->launches = P->graph_launches;
+    } else if (key == P->last_key) {   // second identical request in a row: capture, then replay
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int64_t L = 0;
+        try {
+            L = launch_sequence(P, st, d_in, dtype, a);
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        CK(cudaStreamEndCapture(st, &graph));
+        if (P->gexec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(P->gexec, graph, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(P->gexec);
+                P->gexec = nullptr;
+            }
+        }
+        cudaError_t e = P->gexec ? cudaSuccess : cudaGraphInstantiate(&P->gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(e);
+        P->graph_key = key;
+        P->graph_launches = L;
+        CK(cudaGraphLaunch(P->gexec, st));
+        P->launches = L;
+    } else {
+        P->launches = launch_sequence(P, st, d_in, dtype, a);
+    }
+    P->last_key = key;
     P->last_n = n;
     P->last_flags = flags;
     P->req_prns.assign(prns, prns + n);
@@ -1377,6 +1434,7 @@ int acq_plan_destroy(acq_plan* P) {
                       &P->dftB, &P->dreq})
         b->reset();
     P->hstage.reset();
+    if (P->gexec) cudaGraphExecDestroy(P->gexec);
     for (int i = 0; i < 2; ++i) {
         P->hreq[i].reset();
         if (P->hreq_ev[i]) cudaEventDestroy(P->hreq_ev[i]);
@@ -1611,6 +1669,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
 int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* effective) {
     return guarded([&] {
         if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        ++P->version;   // a replayed launch sequence must be captured again
         if (option == ACQ_OPT_ROTATION_PRECISION) {
             if (value < ACQ_PREC_FP32 || value > ACQ_PREC_BF16_SPLIT)
                 throw AcqError(ACQ_ERR_ARGUMENT, "unknown precision " + std::to_string(value));

@@ -816,6 +816,12 @@ def main():
     flops["fused"] = flops["tile"] + flops["column"]
     ab = alg_bytes.get(name)
     achieved = ab / per_acq_s / 1e9 if ab else None
+    # nominal FP32 (non-tensor) peak: SMs x 128 lanes x 2 (FMA) x the SM clock seen under load
+    props = torch.cuda.get_device_properties(local_rank)
+    sm_clock = clocks.get("sm_max_mhz") or clocks.get("sm_mhz")
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_clock * 1e6 / 1e12 if sm_clock else None
+    fp32_rate = (flops[name] / per_acq_s / 1e12) if name in flops else None
+    step_bytes = sum(v for k, v in alg_bytes.items() if k in ktimes and k != "fused")
     tps = ncu_traffic(name, WORKLOAD)
     roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": (achieved / hbm_peak) if achieved else None,
@@ -824,7 +830,12 @@ def main():
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in pk else "fallback",
             "per_launch_ms": per_launch_s * 1e3, "launches_per_step": nl / args.steps,
             "algorithmic_bytes_per_step": ab,
-            "fp32_tflops": (flops[name] / per_acq_s / 1e12) if name in flops else None,
+            "fp32_tflops": fp32_rate,
+            "fp32_peak_tflops": fp32_peak,
+            "fp32_frac": (fp32_rate / fp32_peak) if (fp32_rate and fp32_peak) else None,
+            "fp32_note": "FLOPs counted at 5 N log2 N per complex FFT; peak = SMs x 128 x 2 x max SM clock (nominal)",
+            # whole step: compulsory bytes of every stage / step time, against the same HBM peak
+            "step_hbm_frac": (step_bytes / t_step / 1e9 / hbm_peak) if step_bytes else None,
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()}}
 
     cpu = None
