@@ -124,7 +124,8 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled every 50 ms during the timed region (the sampler
+    is running, with a first sample taken, before the region starts; only later samples count)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -134,13 +135,18 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.f = None
+        self.skip = 0
 
     def __enter__(self):
         try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
+            t0 = time.time()
+            while time.time() - t0 < 3.0 and os.path.getsize(self.f.name) == 0:
+                time.sleep(0.01)
+            self.skip = sum(1 for _ in open(self.f.name))
         except Exception:
             self.proc = None
         return self
@@ -163,6 +169,8 @@ class ClockSampler:
             if len(parts) >= 9:
                 rows.append(parts)
         os.unlink(self.f.name)
+        if len(rows) > self.skip:
+            rows = rows[self.skip:]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -283,16 +291,21 @@ def run_reference(args):
     if args.config == "cfg5":
         return run_reference_fine(args)
     ci16, _ = make_input()
+    warm = []
     for _ in range(args.warmup):
-        cpu_port_time_per_prn(ci16, 1)
-    times = cpu_port_time_per_prn(ci16, args.steps)
+        warm += cpu_port_time_per_prn(ci16, 1)
+    # each step times one bounded sample; the number of timed samples is capped so the whole run
+    # stays within about two minutes of host time whatever --steps is
+    per_sample = min(warm) if warm else cpu_port_time_per_prn(ci16, 1)[0]
+    n_timed = max(1, min(args.steps, int(120.0 / max(per_sample, 1e-3))))
+    times = cpu_port_time_per_prn(ci16, n_timed)
     per_acq = statistics.mean(times) * cpu_port_sample()[1]
     value = 1.0 / per_acq
     cores = os.cpu_count()
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_acq * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "impl": "reference",
+            "impl": "reference", "timed_samples": n_timed,
             "config": {"workload": WORKLOAD, "prns": 32, "samples": int(len(ci16))},
             "cpu_baseline": {"value": value, "unit": "acq/s", "cores": cores, "kind": "port",
                              "sample": f"1 PRN x {cpu_port_sample()[0]} accumulation step(s) per step, extrapolated to "
@@ -575,7 +588,7 @@ def run_fine(args, world, rank, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")

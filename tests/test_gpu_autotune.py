@@ -145,3 +145,23 @@ def test_option_validation():
     with pytest.raises(A.ArgumentError):
         plan.set_option(6, 258)         # column width above 256
     assert plan.get_option(0) in (0, 1)
+
+
+def test_repeated_requests_replay_the_same_results():
+    # the second identical request captures the launch sequence as a CUDA graph and later ones
+    # replay it; an option change or another input buffer leads back to a fresh capture
+    plan, x = _case()
+    dev = torch.as_tensor(x, device="cuda")
+    runs = [A.acquire_device(plan, dev, list(range(1, 11)), store_power_bins=True) for _ in range(4)]
+    ref = [(r.peak_doppler_bin, r.peak_code_bin, np.asarray(r.power_bins).copy()) for r in runs[0]]
+    for out in runs[1:]:
+        for a, r in zip(ref, out):
+            assert a[:2] == (r.peak_doppler_bin, r.peak_code_bin)
+            assert np.array_equal(a[2], np.asarray(r.power_bins))
+    assert plan.set_option(4, 2) == 2          # tile blocks per round: same sums, new capture
+    dev2 = dev.clone()                          # another input buffer
+    for sig in (dev, dev, dev2, dev2, dev2):
+        out = A.acquire_device(plan, sig, list(range(1, 11)), store_power_bins=True)
+        for a, r in zip(ref, out):
+            assert a[:2] == (r.peak_doppler_bin, r.peak_code_bin)
+            assert np.array_equal(a[2], np.asarray(r.power_bins))
