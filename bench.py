@@ -232,7 +232,9 @@ def run_reference_batch(args):
 
     times = {k: [time_group(k)] for k in groups}
     keys = sorted(groups)
-    for i in range(args.steps):
+    mean_group = statistics.mean(v[0] for v in times.values())
+    n_timed = max(1, min(args.steps, int(120.0 / max(mean_group, 1e-3))))   # about two minutes at most
+    for i in range(n_timed):
         k = keys[i % len(keys)]
         times[k].append(time_group(k))
     t_batch = sum(count[k] * statistics.mean(times[k]) for k in groups)
@@ -241,7 +243,7 @@ def run_reference_batch(args):
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s (32-PRN equivalents)",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded ragged batch)", "impl": "reference",
+            "data": "synthetic (seeded ragged batch)", "impl": "reference", "timed_samples": n_timed,
             "config": {"workload": WORKLOAD, "recordings": len(recs), "prn_acquisitions": n_prn_acq},
             "cpu_baseline": {"value": value, "unit": "acq/s (32-PRN equivalents)", "cores": os.cpu_count(),
                              "kind": "port",
@@ -269,14 +271,14 @@ def run_reference_fine(args):
         O.newton_refine(x, G.GPSL1CA, int(prn[i]), FS, tau[i], dop[i], max_iter=20)
         return time.perf_counter() - t0
 
-    for _ in range(args.warmup):
-        one(int(rng.integers(prn.size)))
-    ts = [one(int(rng.integers(prn.size))) for _ in range(args.steps)]
+    warm = [one(int(rng.integers(prn.size))) for _ in range(max(1, args.warmup))]
+    n_timed = max(1, min(args.steps, int(120.0 / max(min(warm), 1e-3))))   # about two minutes at most
+    ts = [one(int(rng.integers(prn.size))) for _ in range(n_timed)]
     value = 1.0 / statistics.mean(ts)
     line = {"metric": "fine-search cells/s", "value": value, "unit": "cells/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded, CF32, 32 PRNs present)", "impl": "reference",
+            "data": "synthetic (seeded, CF32, 32 PRNs present)", "impl": "reference", "timed_samples": n_timed,
             "config": {"workload": WORKLOAD, "cells": int(prn.size), "samples": int(n)},
             "cpu_baseline": {"value": value, "unit": "cells/s", "cores": 1, "kind": "port",
                              "sample": "FP64 numpy correlator oracle, one random cell per step (forward with "
