@@ -155,6 +155,25 @@ function cfar_threshold(pfa, num_cells; num_noncoherent_integrations = 1)
     out[]
 end
 
+# ---- plan options (ACQ_OPT_* of include/acqgb300.h: launch shapes, kernel form, precision) ----
+const OPTIONS = Dict(:form => 0, :rotation_precision => 1, :mma_scale_log2 => 2, :tile_threads => 3,
+                     :tile_blocks => 4, :tile_pad => 5, :column_width => 6, :column_ctas_per_sm => 7,
+                     :doppler_precision => 8, :tile_rows => 9)
+
+"Set a plan option; returns the value in effect (launch shapes change results only within FP32 rounding)."
+function set_option!(plan::AcquisitionPlan, opt::Symbol, value::Integer)
+    eff = Ref{Int64}(0)
+    check(ccall((:acq_plan_set_option, lib), Cint, (Ptr{Cvoid}, Int32, Int64, Ref{Int64}), plan.h, OPTIONS[opt],
+                value, eff))
+    eff[]
+end
+
+function get_option(plan::AcquisitionPlan, opt::Symbol)
+    v = Ref{Int64}(0)
+    check(ccall((:acq_plan_get_option, lib), Cint, (Ptr{Cvoid}, Int32, Ref{Int64}), plan.h, OPTIONS[opt], v))
+    v[]
+end
+
 # ---- tensor-core precision option ----
 const PRECISIONS = Dict(:fp32 => 0, :fp16 => 1, :bf16 => 2, :fp16_split => 3, :bf16_split => 4)
 
