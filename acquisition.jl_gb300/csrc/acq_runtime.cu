@@ -1659,6 +1659,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_TILE_BLOCKS: *value = P->tile_fs ? P->tileNF : 0; break;
             case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->tileBase : 0; break;
             case ACQ_OPT_TILE_ROWS: *value = P->tile_fs ? P->tileRows : 0; break;
+            case ACQ_OPT_TRANSFORM_LENGTH: *value = P->g.fft_tile; break;
             case ACQ_OPT_COLUMN_WIDTH: *value = P->col_k1 ? P->k1W : P->col_tma ? P->tmaW : 0; break;
             case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_k1 ? P->k1CtasPerSm : P->col_tma ? P->tmaCtasPerSm : 0; break;
             default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
@@ -1669,6 +1670,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
 int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* effective) {
     return guarded([&] {
         if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
+        if (option == ACQ_OPT_TRANSFORM_LENGTH) throw AcqError(ACQ_ERR_ARGUMENT, "the transform length is read-only");
         ++P->version;   // a replayed launch sequence must be captured again
         if (option == ACQ_OPT_ROTATION_PRECISION) {
             if (value < ACQ_PREC_FP32 || value > ACQ_PREC_BF16_SPLIT)

@@ -182,6 +182,8 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_OPT_DOPPLER_PRECISION 8  /* simple path: the per-column Doppler DFT as a dense DFT-matrix GEMM on the
                                         tensor cores (ACQ_PREC_*; ndop <= 250), or FP32 FFTs (default) */
 #define ACQ_OPT_TILE_ROWS 9          /* coherent-tile kernel: rows sharing g mod num_blocks per CTA (1 or 2) */
+#define ACQ_OPT_TRANSFORM_LENGTH 10  /* read-only: length of the block and tile transforms (>= 2 block_size;
+                                        fft_size, or a power of two or five times one up to 5 % longer) */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
  * form is used only where the plan's sizes have a fused kernel (otherwise plain).

@@ -255,3 +255,32 @@ def test_repeated_prns_up_to_the_plan_size():
     assert (a.peak_doppler_bin, a.peak_code_bin, a.noise_power) == (b.peak_doppler_bin, b.peak_code_bin, b.noise_power)
     with pytest.raises(A.ArgumentError, match="at most 3 PRNs"):
         A.acquire_b(plan, x, [1, 2, 3, 1])
+
+
+# Simple-path geometries that reach each transform length the runtime may pick (512, 1024, 1280,
+# 2560, 256 for fft_size 500, 1000, 1250, 2500, 250) and each code-block count of the
+# Doppler-group column stage (nb = 8, 10, 16, 25, 40, 50, 64), with two or four coherent periods
+# (first Doppler pass on the spectra, two tile rows per CTA) and a longer accumulation (drift halo).
+TRANSFORM_CASES = [
+    # (fs, n_coh, n_nc, coverage, doppler of the planted satellite, nb, transform length)
+    (4e6, 2, 2, 3000, 700.0, 8, 1024),
+    (5e6, 2, 2, 4000, -900.0, 10, 1024),
+    (4e6, 2, 2, 5000, 1300.0, 16, 512),
+    (12.5e6, 2, 2, 10000, -2100.0, 25, 1024),
+    (8e6, 2, 2, 25000, 4100.0, 64, 256),
+    (10e6, 2, 2, 16000, -3300.0, 40, 512),
+    (12.5e6, 2, 2, 16000, 5200.0, 50, 512),
+    (10e6, 2, 2, 5000, 1800.0, 16, 1280),
+    (25e6, 2, 2, 5000, -1200.0, 20, 2560),
+    (10e6, 4, 4, 16000, 6900.0, 40, 512),    # 16 coherent periods of drift
+]
+
+
+@pytest.mark.parametrize("fs,n_coh,n_nc,cov,dop,nb,length", TRANSFORM_CASES)
+def test_transform_lengths_and_doppler_groups(fs, n_coh, n_nc, cov, dop, nb, length):
+    sats = [synth.Satellite(1, 47.0, dop, 417.25)]
+    plan, res, outs = _run_case("GPSL1CA", fs, [1, 2], n_coh=n_coh, n_nc=n_nc, cov=cov, sats=sats, seed=29)
+    assert plan.geometry.num_blocks == nb
+    assert plan.get_option(10) == length          # ACQ_OPT_TRANSFORM_LENGTH
+    assert plan.get_option(6) == 128              # the Doppler-group column stage's default width
+    _compare(res, outs, f"fs={fs} n_coh={n_coh} n_nc={n_nc} cov={cov}")
