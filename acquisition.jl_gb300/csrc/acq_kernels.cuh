@@ -352,10 +352,6 @@ __global__ void k_col_rot(const float2* __restrict__ T, int ndop, int spc, int W
 // Peak with the reference tie-break, FP64 noise sums. Materialised order (lowest effective
 // column, then lowest row: src/est_signal_noise_power.jl:109-135); streamed rotation order
 // (code-phase column, rotation slice, row: src/acquire.jl:306-324).
-__device__ __forceinline__ unsigned long long peak_key(float v, uint32_t order) {
-    return (static_cast<unsigned long long>(__float_as_uint(v)) << 32) |
-           static_cast<unsigned long long>(0xFFFFFFFFu - order);
-}
 
 constexpr int kStatsCols = 256;  // columns per stats CTA
 
@@ -435,6 +431,9 @@ __global__ void k_stats(const float* __restrict__ acc, int ndop, int ncols, int 
 struct ExtractParams {
     int ndop, spc, spc_eff, nb, bs, R, n_coh, ndb, n_be, n_nc, path, combos, n_pat;
     int streamed_rot, noise_estimator, samples_per_chip, interp, nct;
+    // npk peak keys per PRN; rowmode 1: no column sums (the statistics came from the column
+    // stage), the global mean is the total of the row sums minus the columns near the peak
+    int npk, rowmode;
     double fs, fc, code_length, t_coh, doppler_first, doppler_step, cfar_thr;
 };
 
@@ -460,8 +459,8 @@ __global__ void k_extract(const float* __restrict__ acc, const uint16_t* __restr
     __shared__ unsigned long long kred[256];
     const int pi = blockIdx.x;
     unsigned long long best = 0ULL;
-    for (int i = threadIdx.x; i < P.nct; i += blockDim.x) {
-        unsigned long long k = peakpart[static_cast<int64_t>(pi) * P.nct + i];
+    for (int i = threadIdx.x; i < P.npk; i += blockDim.x) {
+        unsigned long long k = peakpart[static_cast<int64_t>(pi) * P.npk + i];
         best = k > best ? k : best;
     }
     kred[threadIdx.x] = best;
@@ -489,8 +488,19 @@ __global__ void k_extract(const float* __restrict__ acc, const uint16_t* __restr
     if (P.noise_estimator == ACQ_NOISE_GLOBAL_MEAN) {
         lo = max(0, col - P.samples_per_chip);
         hi = min(P.spc_eff - 1, col + P.samples_per_chip);
-        for (int c = threadIdx.x; c < P.spc_eff; c += blockDim.x)
-            if (c < lo || c > hi) part += colsum[static_cast<int64_t>(pi) * P.spc_eff + c];
+        if (P.rowmode) {
+            const float* apk = acc + static_cast<int64_t>(pi) * P.ndop * P.spc_eff;
+            for (int i = threadIdx.x; i < P.nct * P.ndop; i += blockDim.x)
+                part += rowpart[static_cast<int64_t>(pi) * P.nct * P.ndop + i];
+            const int w = hi - lo + 1;
+            for (int i = threadIdx.x; i < w * P.ndop; i += blockDim.x) {
+                const int r = i / w, c = lo + (i - r * w);
+                part -= static_cast<double>(apk[static_cast<int64_t>(r) * P.spc_eff + c]);
+            }
+        } else {
+            for (int c = threadIdx.x; c < P.spc_eff; c += blockDim.x)
+                if (c < lo || c > hi) part += colsum[static_cast<int64_t>(pi) * P.spc_eff + c];
+        }
     } else {
         const int opp = (row + P.ndop / 2) % P.ndop;
         for (int i = threadIdx.x; i < P.nct; i += blockDim.x)

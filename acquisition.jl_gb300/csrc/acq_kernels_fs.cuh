@@ -215,9 +215,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
+// Peak key with the reference tie-break: float bits above the complemented scan order, so the
+// largest key is the largest value and, among equal values, the first in scan order.
+__device__ __forceinline__ unsigned long long peak_key(float v, uint32_t order) {
+    return (static_cast<unsigned long long>(__float_as_uint(v)) << 32) |
+           static_cast<unsigned long long>(0xFFFFFFFFu - order);
+}
+
 struct ColTmaParams {
     int spc, spc_eff, n_nc, W, halo, box_rows, n_boxes, n_items, n_cblk, rows_per_step;
     int n1;                // pass-2 FFTs per column when the first pass was applied to the spectra
+    // k_col_tma_k1 only, when non-null: per-item statistics for the extraction (FP64 row sums of
+    // everything the item adds to a row; the peak key of the cells it stores), npk keys per PRN
+    double* rowpart;
+    unsigned long long* peakpart;
+    int npk;
     const float2* twD;
     const int* drift;      // (n_nc, ndop) in [0, spc)
     float* acc;            // (n_req, ndop, spc_eff)
@@ -355,6 +367,11 @@ __global__ void __launch_bounds__(256) k_col_tma(const __grid_constant__ CUtenso
     }
 }
 
+// Row-sum slot of (requested PRN pi, column block cb) in the per-item statistics.
+__device__ __forceinline__ double* rowpart_item(const ColTmaParams& p, int pi, int cb, int nd) {
+    return p.rowpart + (static_cast<int64_t>(pi) * p.n_cblk + cb) * nd;
+}
+
 // PRE-mode column stage by Doppler group: output (k1, k2) of a column needs only the nb tile rows
 // k1 * nb + k (k < nb), so a work item is (requested PRN, k1, block of W columns) and its tile is
 // nb rows x W columns: each row segment is W * 8 contiguous bytes (1 KB at W = 128) instead of the
@@ -449,19 +466,56 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
         if (m == p.n_nc - 1) {
             float* ap = p.acc + static_cast<int64_t>(pi) * ND * p.spc_eff;
             const int span = wv + 2 * H;
-            for (int k2 = threadIdx.x / 32; k2 < N2; k2 += blockDim.x / 32) {
-                float* arow = ap + static_cast<int64_t>(rowof[k2]) * p.spc_eff;
-                for (int j = threadIdx.x & 31; j < span; j += 32) {
+            const int lane = threadIdx.x & 31, warp = threadIdx.x / 32;
+            // the largest stored value of this lane and its scan order (the smaller order wins a tie)
+            float bv = -1.f;
+            uint32_t bo = 0xFFFFFFFFu;
+            for (int k2 = warp; k2 < N2; k2 += blockDim.x / 32) {
+                const int row = rowof[k2];
+                float* arow = ap + static_cast<int64_t>(row) * p.spc_eff;
+                float rs = 0.f;
+                for (int j = lane; j < span; j += 32) {
                     const int lc = j - H;
                     float* src = accs + k2 * AW + H + lc;
                     const float v = *src;
                     *src = 0.f;
+                    rs += v;
                     int c = c0 + lc;
                     if (c < 0) c += p.spc;
                     if (c >= p.spc) c -= p.spc;
-                    if (H == 0 || (lc >= H && lc < wv - H)) arow[c] = v;
-                    else if (v != 0.f) atomicAdd(arow + c, v);
+                    if (H == 0 || (lc >= H && lc < wv - H)) {
+                        arow[c] = v;
+                        const uint32_t ord = static_cast<uint32_t>(c) * ND + row;
+                        if (v > bv || (v == bv && ord < bo)) {
+                            bv = v;
+                            bo = ord;
+                        }
+                    } else if (v != 0.f) {
+                        atomicAdd(arow + c, v);
+                    }
                 }
+                if (p.rowpart) {   // FP32 across the warp, FP64 across column blocks (in the extraction)
+                    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
+                    if (lane == 0) rowpart_item(p, pi, cb, ND)[row] = static_cast<double>(rs);
+                }
+            }
+            if (p.peakpart) {
+                unsigned long long best = bv >= 0.f ? peak_key(bv, bo) : 0ULL;
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+                    best = other > best ? other : best;
+                }
+                unsigned long long* kred = reinterpret_cast<unsigned long long*>(accs);   // free until the next item
+                __syncthreads();
+                if (lane == 0) kred[warp] = best;
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    unsigned long long b = kred[0];
+                    for (int w = 1; w < static_cast<int>(blockDim.x / 32); ++w) b = kred[w] > b ? kred[w] : b;
+                    p.peakpart[static_cast<int64_t>(pi) * p.npk + k1 * p.n_cblk + cb] = b;
+                }
+                __syncthreads();
+                if (threadIdx.x < blockDim.x / 32) kred[threadIdx.x] = 0ULL;   // the accumulator starts at zero
             }
             __syncthreads();
         }

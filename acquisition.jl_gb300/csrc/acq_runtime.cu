@@ -106,6 +106,38 @@ __global__ void k_gather_cols(const float* __restrict__ in, int64_t rows, int64_
     }
 }
 
+// Peak keys of the accumulator cells the Doppler-group column stage adds to atomically (the
+// columns within H of a column-block boundary: multiples of W, and spc, wrapping to 0), whose
+// final values exist only once that stage has finished. One CTA per (boundary, requested PRN);
+// key j of the PRN's slots after `slot0`.
+__global__ void k_edge_peaks(const float* __restrict__ acc, int ndop, int spc, int spc_eff, int W, int H, int n_bound,
+                             int slot0, int npk, unsigned long long* __restrict__ peakpart) {
+    __shared__ unsigned long long kred[8];
+    const int j = blockIdx.x, pi = blockIdx.y;
+    const int b = j == n_bound - 1 ? spc : j * W;
+    const float* ap = acc + static_cast<int64_t>(pi) * ndop * spc_eff;
+    unsigned long long best = 0ULL;
+    for (int i = threadIdx.x; i < ndop * 2 * H; i += blockDim.x) {
+        const int r = i / (2 * H), o = i - r * 2 * H - H;
+        int c = b + o;
+        if (c < 0) c += spc;
+        if (c >= spc) c -= spc;
+        const unsigned long long key = peak_key(ap[static_cast<int64_t>(r) * spc_eff + c], static_cast<uint32_t>(c) * ndop + r);
+        best = key > best ? key : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, best, o);
+        best = other > best ? other : best;
+    }
+    if ((threadIdx.x & 31) == 0) kred[threadIdx.x / 32] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = kred[0];
+        for (int w = 1; w < static_cast<int>(blockDim.x / 32); ++w) m = kred[w] > m ? kred[w] : m;
+        peakpart[static_cast<int64_t>(pi) * npk + slot0 + j] = m;
+    }
+}
+
 // Zeroes the accumulator cells that the TMA column stages add to atomically: the columns within
 // H of a column-block boundary (multiples of W, and spc, wrapping to 0). Every other cell is
 // stored by exactly one work item, so the accumulator needs no full clear.
@@ -535,6 +567,11 @@ void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
     }
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device));
+    // per-item statistics of this form: row sums per column block, and a peak key per item plus
+    // one per block boundary
+    const int n_cblk = (g.spc + W - 1) / W;
+    P->rowpart.ensure(sizeof(double) * (size_t)n_prns * n_cblk * g.ndop);
+    P->peakpart.ensure(sizeof(unsigned long long) * (size_t)n_prns * (g.n_coh * n_cblk + n_cblk + 1));
     P->tmapK1 = map;
     P->col_k1 = fn;
     P->k1W = W;
@@ -877,6 +914,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     const int use_if = a.use_if;
     const float if_step = a.if_step;
     int64_t L = 0;
+    int stats_nct = 0, stats_npk = 0;   // set when the column stage produced the statistics
     const int G = g.n_coh * g.nb;
     t_begin(P, ACQ_KERNEL_FRONTEND);
     k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF, P->S.as<float2>(),
@@ -947,14 +985,31 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             cp.W = P->k1W;
             cp.n_cblk = (g.spc + P->k1W - 1) / P->k1W;
             cp.n_items = n * g.n_coh * cp.n_cblk;
+            // the extraction's statistics come from this stage (no separate pass over the surface)
+            const int n_bound = cp.n_cblk + 1;
+            cp.rowpart = P->rowpart.as<double>();
+            cp.peakpart = P->peakpart.as<unsigned long long>();
+            cp.npk = g.n_coh * cp.n_cblk + (P->tmaH > 0 ? n_bound : 0);
             const int grid = std::max(1, std::min(P->k1Grid, cp.n_items));
             P->col_k1<<<grid, 128, P->smem_col_k1, st>>>(P->tmapK1, cp);
+            t_end(P);
+            ++L;
+            if (P->tmaH > 0) {
+                t_begin(P, ACQ_KERNEL_STATS);
+                k_edge_peaks<<<dim3(n_bound, n), 128, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc, g.spc_eff, P->k1W,
+                                                              P->tmaH, n_bound, g.n_coh * cp.n_cblk, cp.npk,
+                                                              P->peakpart.as<unsigned long long>());
+                t_end(P);
+                ++L;
+            }
+            stats_nct = cp.n_cblk;
+            stats_npk = cp.npk;
         } else {
             const int grid = std::max(1, std::min(P->tmaGrid, cp.n_items));
             P->col_tma<<<grid, kThreads, P->smem_col_tma, st>>>(P->tmapT, cp);
+            t_end(P);
+            ++L;
         }
-        t_end(P);
-        ++L;
     }
     for (int m = 0; m < ((use_fused || use_tma) ? 0 : g.n_nc); ++m) {
         const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_tile;
@@ -1044,12 +1099,14 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         ++L;
     }
     const int streamed_rot = (g.n_nc == 1 && g.R > 1) ? 1 : 0;
-    t_begin(P, ACQ_KERNEL_STATS);
-    k_stats<<<dim3(P->nct, n), kThreads, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc_eff, g.spc, g.R, streamed_rot,
-                                                  P->rowpart.as<double>(), P->colsum.as<double>(),
-                                                  P->peakpart.as<unsigned long long>());
-    t_end(P);
-    ++L;
+    if (stats_npk == 0) {
+        t_begin(P, ACQ_KERNEL_STATS);
+        k_stats<<<dim3(P->nct, n), kThreads, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc_eff, g.spc, g.R, streamed_rot,
+                                                      P->rowpart.as<double>(), P->colsum.as<double>(),
+                                                      P->peakpart.as<unsigned long long>());
+        t_end(P);
+        ++L;
+    }
     ExtractParams EP{};
     EP.ndop = g.ndop; EP.spc = g.spc; EP.spc_eff = g.spc_eff; EP.nb = g.nb; EP.bs = g.bs; EP.R = g.R;
     EP.n_coh = g.n_coh; EP.ndb = g.ndb; EP.n_be = g.n_be; EP.n_nc = g.n_nc; EP.path = g.path;
@@ -1057,7 +1114,9 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     EP.noise_estimator = g.noise_estimator;
     EP.samples_per_chip = static_cast<int>(std::floor(P->desc.sampling_freq_hz / P->sys->code_freq));
     EP.interp = (flags & ACQ_FLAG_SUBSAMPLE_INTERP) ? 1 : 0;
-    EP.nct = P->nct;
+    EP.nct = stats_npk ? stats_nct : P->nct;
+    EP.npk = stats_npk ? stats_npk : P->nct;
+    EP.rowmode = stats_npk ? 1 : 0;
     EP.fs = P->desc.sampling_freq_hz; EP.fc = P->sys->code_freq; EP.code_length = P->sys->code_length;
     EP.t_coh = g.n_coh * (static_cast<double>(P->sys->code_length) / P->sys->code_freq);
     EP.doppler_first = g.doppler_first; EP.doppler_step = g.doppler_step; EP.cfar_thr = g.cfar_thr;
