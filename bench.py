@@ -836,7 +836,8 @@ def main():
     sm_clock = clocks.get("sm_max_mhz") or clocks.get("sm_mhz")
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_clock * 1e6 / 1e12 if sm_clock else None
     fp32_rate = (flops[name] / per_acq_s / 1e12) if name in flops else None
-    step_bytes = sum(v for k, v in alg_bytes.items() if k in ktimes and k != "fused")
+    # (the statistics no longer re-read the surface on the simple path: frontend, tile, column)
+    step_bytes = sum(v for k, v in alg_bytes.items() if k in ktimes and k in ("frontend", "tile", "column"))
     tps = ncu_traffic(name, WORKLOAD)
     roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
             "frac": (achieved / hbm_peak) if achieved else None,
