@@ -10,6 +10,8 @@ accumulation sums (results within FP32 rounding, decisions unchanged):
   column_width         ACQ_OPT_COLUMN_WIDTH        code-phase columns per TMA tile
   column_ctas_per_sm   ACQ_OPT_COLUMN_CTAS_PER_SM  persistent column CTAs per SM
   form                 ACQ_OPT_FORM                plain (one kernel per stage) or fused (cluster)
+  tile_mma             ACQ_OPT_TILE_MMA            coherent tile as a tensor-core correlation GEMM (1) or
+                                                   FP32 FFTs (0); results within FP32 rounding
 Reduced-precision rotation combines change results within their stated bounds, so they are
 tuned only on request (``allow_reduced_precision``).
 
@@ -35,7 +37,10 @@ KNOBS = {
     "tile_pad": L.ACQ_OPT_TILE_PAD,
     "column_width": L.ACQ_OPT_COLUMN_WIDTH,
     "column_ctas_per_sm": L.ACQ_OPT_COLUMN_CTAS_PER_SM,
+    "tile_mma": L.ACQ_OPT_TILE_MMA,
 }
+# knobs whose 0 is a setting (for the others 0 means the plan's sizes lack that kernel)
+ZERO_IS_A_VALUE = {"tile_mma"}
 FORMS = {"plain": L.ACQ_FORM_PLAIN, "fused": L.ACQ_FORM_FUSED}
 
 
@@ -45,7 +50,8 @@ def candidates(plan) -> dict:
     blocks = sorted({b for b in (1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 25) if b <= nb})
     rows = [1, 2] if plan.geometry.num_coherently_integrated_code_periods >= 2 else [1]
     return {"tile_rows": rows, "tile_threads": [64, 128, 192, 256], "tile_blocks": blocks, "tile_pad": [0, 1, 9],
-            "column_width": [8, 12, 16, 20, 24, 32, 64, 128, 256], "column_ctas_per_sm": [1, 2, 3, 4, 6], "form": ["plain", "fused"]}
+            "column_width": [8, 12, 16, 20, 24, 32, 64, 128, 256], "column_ctas_per_sm": [1, 2, 3, 4, 6], "form": ["plain", "fused"],
+            "tile_mma": [1, 0]}
 
 
 def current(plan) -> dict:
@@ -61,7 +67,7 @@ def apply(plan, settings: dict) -> dict:
     for k, v in settings.items():
         if k == "form":
             eff[k] = plan.set_form(v)
-        elif k in KNOBS and v:
+        elif k in KNOBS and (v or k in ZERO_IS_A_VALUE):
             try:
                 eff[k] = plan.set_option(KNOBS[k], int(v))
             except Exception:

@@ -18,6 +18,7 @@
 #include "acq_inst.h"
 #include "acq_mma.cuh"
 #include "acq_kernels.cuh"
+#include "acq_tile_mma.cuh"
 
 using namespace acq;
 
@@ -338,6 +339,13 @@ struct acq_plan {
     CUtensorMap tmapK1{};
     int k1W = 128, k1Grid = 1, k1CtasPerSm = 0;
     size_t smem_col_k1 = 0;
+    // coherent tile as a correlation GEMM on the tensor cores (TMA simple path, block size <= 256):
+    // time-domain operand blocks per (step, row), their inverse scales, one CTA per SM
+    bool tmma = false;
+    bool tmma_enabled = true;   // ACQ_OPT_TILE_MMA
+    DevBuf stubs, invsc;
+    int tmmaSms = 1;
+    size_t smem_tmma = 0;
     CUtensorMap tmapT{};
     DevBuf Tall, errflag;
     PinnedBuf hstage;   // fetch staging: error word, then the results
@@ -580,6 +588,25 @@ void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
     P->smem_col_k1 = smem;
 }
 
+// Tensor-core coherent tile (k_tile_mma): used on the TMA simple path when the block size fits
+// its operands (bs <= 256) and ACQ_OPT_TILE_MMA is on. The FP32 FFT tile stays the fallback.
+void setup_tile_mma(acq_plan* P) {
+    const Geometry& g = P->g;
+    P->tmma = false;
+    if (!P->tmma_enabled || !P->col_tma || g.bs > kTmmaMaxBs || getenv_flag("ACQ_NO_TILE_MMA")) return;
+    const int G = g.n_coh * g.nb;
+    const size_t row_bytes = tmma_row_bytes(g.bs);
+    // one CTA per SM: a CTA holds up to 512 tensor-memory columns
+    const size_t smem = std::max<size_t>(tmma_smem_bytes(g.bs), 120 * 1024);
+    if (smem > 227 * 1024) return;
+    P->stubs.ensure(row_bytes * g.n_nc * G);
+    P->invsc.ensure(sizeof(float) * g.n_nc * G);
+    set_smem((const void*)k_tile_mma, smem);
+    CK(cudaDeviceGetAttribute(&P->tmmaSms, cudaDevAttrMultiProcessorCount, P->device));
+    P->smem_tmma = smem;
+    P->tmma = true;
+}
+
 // TMA-staged column stage: T for all steps in HBM, a tensor map over it, a persistent grid.
 void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     const Geometry& g = P->g;
@@ -653,7 +680,7 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->tmaH = H;
     P->smem_col_tma = smem;
     if (pre) setup_col_k1(P, n_prns, P->k1W, P->k1CtasPerSm);
-
+    setup_tile_mma(P);
 }
 
 void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
@@ -916,12 +943,17 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     int64_t L = 0;
     int stats_nct = 0, stats_npk = 0;   // set when the column stage produced the statistics
     const int G = g.n_coh * g.nb;
-    t_begin(P, ACQ_KERNEL_FRONTEND);
-    k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF, P->S.as<float2>(),
-                                                            use_if, if_step, a.d_if_off);
-    t_end(P);
-    ++L;
     const bool use_fused = P->fused && P->form == ACQ_FORM_FUSED;
+    const bool use_tma = !use_fused && P->col_tma != nullptr && P->dft_mma == nullptr;
+    // the tensor-core tile reads the samples itself: no block spectra
+    const bool use_tmma = use_tma && P->tmma;
+    if (!use_tmma) {
+        t_begin(P, ACQ_KERNEL_FRONTEND);
+        k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF,
+                                                                P->S.as<float2>(), use_if, if_step, a.d_if_off);
+        t_end(P);
+        ++L;
+    }
     if (use_fused) {
         if (P->fusedH > 0)
             CK(cudaMemsetAsync(P->accb.p, 0, sizeof(float) * (size_t)n * g.ndop * g.spc_eff, st));
@@ -947,12 +979,33 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         t_end(P);
         ++L;
     }
-    const bool use_tma = !use_fused && P->col_tma != nullptr && P->dft_mma == nullptr;
+    if (use_tmma) {
+        // operand blocks of every (step, row), then the correlation GEMM for all steps
+        const int nprn = static_cast<int>(P->prns.size());
+        t_begin(P, ACQ_KERNEL_FRONTEND);
+        k_tile_stubs<<<dim3(G, g.n_nc), kTmmaStubThreads, 0, st>>>(
+            d_in, dtype, seg_len, G, g.nb, g.n_coh, g.bs, P->col_pre ? 1 : 0, use_if, if_step, a.d_if_off,
+            P->fftD.tw, P->stubs.as<uint8_t>(), P->invsc.as<float>());
+        t_end(P);
+        ++L;
+        TileMmaParams tp{};
+        tp.stubs = P->stubs.as<uint8_t>(); tp.inv_scale = P->invsc.as<float>(); tp.codes = P->codes.as<int8_t>();
+        tp.slots = a.d_slots; tp.T = P->Tall.as<float2>(); tp.t_step_stride = static_cast<int64_t>(nprn) * G * g.spc;
+        tp.n = n; tp.G = G; tp.nb = g.nb; tp.bs = g.bs; tp.spc = g.spc;
+        tp.n_chunks = (n * g.nb + kTmmaRows - 1) / kTmmaRows;
+        tp.units = g.n_nc * G;
+        tp.cpc = std::max(1, std::min(tp.units, P->tmmaSms / tp.n_chunks));
+        tp.err = P->errflag.as<int>();
+        t_begin(P, ACQ_KERNEL_TILE);
+        k_tile_mma<<<tp.n_chunks * tp.cpc, kTmmaThreads, P->smem_tmma, st>>>(tp);
+        t_end(P);
+        ++L;
+    }
     if (use_tma) {
         // coherent tiles of every step in one launch, then the TMA-staged column stage
         const int nprn = static_cast<int>(P->prns.size());
         const float2* spectra = P->S.as<float2>();
-        if (P->col_pre && g.n_coh > 1) {   // one coherent period: the first pass is the identity
+        if (!use_tmma && P->col_pre && g.n_coh > 1) {   // one coherent period: the first pass is the identity
             t_begin(P, ACQ_KERNEL_FRONTEND);
             k_doppler_prepass<<<dim3((g.fft_tile + 127) / 128, g.nb * g.n_coh, g.n_nc), 128, 0, st>>>(
                 P->S.as<float2>(), P->U.as<float2>(), G, g.nb, g.n_coh, g.fft_tile, P->fftD.tw);
@@ -960,12 +1013,14 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             ++L;
             spectra = P->U.as<float2>();
         }
-        t_begin(P, ACQ_KERNEL_TILE);
-        P->tile_fs<<<dim3(tile_grid_x(P), n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
-            spectra, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
-            P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
-        t_end(P);
-        ++L;
+        if (!use_tmma) {
+            t_begin(P, ACQ_KERNEL_TILE);
+            P->tile_fs<<<dim3(tile_grid_x(P), n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
+                spectra, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
+                P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
+            t_end(P);
+            ++L;
+        }
         if (P->tmaH > 0) {
             const int wc = P->col_k1 ? P->k1W : P->tmaW;
             const int n_bound = (g.spc + wc - 1) / wc + 1;
@@ -1719,6 +1774,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_TILE_PAD: *value = P->tile_fs ? P->tileFS - P->tileBase : 0; break;
             case ACQ_OPT_TILE_ROWS: *value = P->tile_fs ? P->tileRows : 0; break;
             case ACQ_OPT_TRANSFORM_LENGTH: *value = P->g.fft_tile; break;
+            case ACQ_OPT_TILE_MMA: *value = P->tmma ? 1 : 0; break;
             case ACQ_OPT_COLUMN_WIDTH: *value = P->col_k1 ? P->k1W : P->col_tma ? P->tmaW : 0; break;
             case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_k1 ? P->k1CtasPerSm : P->col_tma ? P->tmaCtasPerSm : 0; break;
             default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
@@ -1868,6 +1924,14 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
                 P->dft_prec = static_cast<int>(value);
             }
             if (effective) *effective = P->dft_prec;
+            return;
+        }
+        if (option == ACQ_OPT_TILE_MMA) {
+            if (value != 0 && value != 1) throw AcqError(ACQ_ERR_ARGUMENT, "tile MMA must be 0 or 1");
+            CK(cudaStreamSynchronize(P->stream));
+            P->tmma_enabled = value != 0;
+            setup_tile_mma(P);
+            if (effective) *effective = P->tmma ? 1 : 0;
             return;
         }
         if (option == ACQ_OPT_MMA_SCALE_LOG2) {

@@ -671,7 +671,7 @@ def main():
         from acqgb300 import autotune as T
         tuned = T.tune(plan, dev, PRNS, reps=3, passes=1, store=False,
                        knobs=("tile_rows", "tile_threads", "tile_blocks", "tile_pad", "column_width",
-                              "column_ctas_per_sm"))
+                              "column_ctas_per_sm", "tile_mma"))
 
     # warm-up (device-resident and public API)
     for _ in range(args.warmup):
@@ -811,10 +811,16 @@ def main():
     spc_eff = g.samples_per_code_eff
     # algorithmic bytes of each kernel class per acquisition (compulsory HBM traffic of the form):
     # the coherent tile is written once and read once per step, the accumulator written once
+    tile_mma = plan.get_option(11) == 1
+    bs = g.block_size
+    # tensor-core tile operands: per (step, row) the Q_s blocks of Re/Im hi/lo (FP16)
+    ks, nh = (bs + 15) // 16, (bs + 127) // 128
+    stub_bytes = 4 * (2 * ks + 16 * nh - 1) * 128
     alg_bytes = {
-        "tile": n_nc * (n_prn * ndop * spc * 8 + ndop * F * 8) + n_prn * nb * F * 8,
+        "tile": (n_nc * (n_prn * ndop * spc * 8 + ndop * stub_bytes) + n_prn * spc if tile_mma else
+                 n_nc * (n_prn * ndop * spc * 8 + ndop * F * 8) + n_prn * nb * F * 8),
         "column": n_nc * n_prn * ndop * spc * 8 + n_prn * ndop * spc_eff * 4,
-        "frontend": n_nc * N_COH * spc * ci16.itemsize * 2 + n_nc * ndop * F * 8,
+        "frontend": n_nc * N_COH * spc * ci16.itemsize * 2 + n_nc * ndop * (stub_bytes if tile_mma else F * 8),
         "stats": n_prn * ndop * spc_eff * 4,
         # fused: input spectra + code spectra reads, one accumulator write (the algorithmic minimum)
         "fused": n_nc * ndop * F * 8 + n_prn * nb * F * 8 + n_prn * ndop * spc_eff * 4,
@@ -824,6 +830,10 @@ def main():
     fft_flops = lambda n: 5.0 * n * math.log2(n)
     n_cand = (g.num_secondary_rotations * (1 << (g.num_data_bits - 1)) * g.bit_edge_search_steps
               if g.path != 0 else 1)
+    # tensor-core tile: MMAs executed (128-row blocks of code rows x 128-lag halves x K, Re and Im,
+    # hi and lo)
+    n_chunks = (n_prn * nb + 127) // 128
+    mma_flops = n_nc * ndop * n_chunks * 128 * nh * 128 * ks * 16 * 2 * 2 * 2
     flops = {
         "tile": n_nc * n_prn * ndop * nb * (fft_flops(F) + 6 * F),
         "column": n_nc * n_prn * spc * n_cand * (fft_flops(ndop) + 3 * ndop),
@@ -835,7 +845,7 @@ def main():
     props = torch.cuda.get_device_properties(local_rank)
     sm_clock = clocks.get("sm_max_mhz") or clocks.get("sm_mhz")
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_clock * 1e6 / 1e12 if sm_clock else None
-    fp32_rate = (flops[name] / per_acq_s / 1e12) if name in flops else None
+    fp32_rate = (flops[name] / per_acq_s / 1e12) if name in flops and not (tile_mma and name == "tile") else None
     # (the statistics no longer re-read the surface on the simple path: frontend, tile, column)
     step_bytes = sum(v for k, v in alg_bytes.items() if k in ktimes and k in ("frontend", "tile", "column"))
     tps = ncu_traffic(name, WORKLOAD)
@@ -850,6 +860,13 @@ def main():
             "fp32_peak_tflops": fp32_peak,
             "fp32_frac": (fp32_rate / fp32_peak) if (fp32_rate and fp32_peak) else None,
             "fp32_note": "FLOPs counted at 5 N log2 N per complex FFT; peak = SMs x 128 x 2 x max SM clock (nominal)",
+            "tile_form": "tensor-core correlation GEMM (FP16 codes x FP16 hi+lo samples, FP32 accumulation)"
+                         if tile_mma else "FP32 four-step FFT",
+            "tile_tensor_tflops": (mma_flops / (ktimes["tile"][0] / args.steps / 1e3) / 1e12
+                                   if tile_mma and "tile" in ktimes else None),
+            "tile_tensor_frac": (mma_flops / (ktimes["tile"][0] / args.steps / 1e3) / 1e12 / pk["bf16_tflops"]
+                                 if tile_mma and "tile" in ktimes and "bf16_tflops" in pk else None),
+            "tile_tensor_note": "MMA FLOPs executed / tile time, against the measured dense bf16 cuBLAS burst peak",
             # whole step: compulsory bytes of every stage / step time, against the same HBM peak
             "step_hbm_frac": (step_bytes / t_step / 1e9 / hbm_peak) if step_bytes else None,
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()}}
