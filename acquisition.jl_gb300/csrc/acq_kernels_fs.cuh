@@ -205,6 +205,17 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// the same load with an L2 evict-first policy (data read once)
+__device__ __forceinline__ void tma_load_2d_ef(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+        "%3}], [%4], %5;" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+
 // Bounded wait on an mbarrier phase: gives up after kWaitLimit polls, records `code` in *err.
 constexpr uint32_t kWaitLimit = 1u << 24;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err, int code,
@@ -411,7 +422,7 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
         const int b = k & 1;
         fence_proxy_async();
         mbar_expect_tx(&mbar[b], tile_bytes);
-        tma_load_2d(buf0 + b * BS, &tmap, cb * W, m * p.rows_per_step + grp * N2, &mbar[b]);
+        tma_load_2d_ef(buf0 + b * BS, &tmap, cb * W, m * p.rows_per_step + grp * N2, &mbar[b]);
     };
     uint32_t phases = 0u;   // bit b: the parity to wait for on mbar[b]
     if (threadIdx.x == 0 && K > 0) issue(0);

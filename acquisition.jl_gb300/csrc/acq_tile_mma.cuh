@@ -29,7 +29,7 @@
 namespace acq {
 
 constexpr int kTmmaRows = 128;      // code rows (PRN, block) per CTA: the MMA's M
-constexpr int kTmmaDrainWarps = 16;
+constexpr int kTmmaDrainWarps = 8;
 constexpr int kTmmaThreads = 32 * kTmmaDrainWarps + 32;   // drain warps + the issuing warp
 constexpr int kTmmaStubThreads = 256;
 
@@ -316,19 +316,23 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
             }
         }
     } else {
-        // drain warps: warp w reads lags 128 h + 32 (w % 4) + lane and code rows 32 (w / 4) .. + 31;
-        // lane l holds the tile offset of code row 32 (w / 4) + l for the current unit
-        const int sp = warp & 3, cbase = (warp >> 2) * 32;
-        const int64_t my_off = col_off[cbase + lane];
-        const int my_m = col_m[cbase + lane];
+        // drain warps: warp w reads lags 128 h + 32 (w % 4) + lane and code rows 64 (w / 4) .. + 63;
+        // lane l holds the tile offsets of code rows 64 (w / 4) + l and + 32 + l for the current unit.
+        // The next 16 columns' tcgen05.ld is in flight while the current ones are stored; the
+        // stores stream (evict-first): the tile is read once, by the Doppler stage, much later.
+        const int sp = warp & 3, cbase = (warp >> 2) * 64;
+        const int64_t my_off = col_off[cbase + lane], my_off2 = col_off[cbase + 32 + lane];
+        const int my_m = col_m[cbase + lane], my_m2 = col_m[cbase + 32 + lane];
         for (int u = 0; u < nu; ++u) {
             const int gu = u0 + u;
             const int step = gu / p.G, rho = gu - (gu / p.G) * p.G;
             int r = my_m - rho % p.nb;
             if (r < 0) r += p.nb;
-            const int64_t off_l = my_off < 0 ? -1
-                                             : step * p.t_step_stride + static_cast<int64_t>(rho) * p.spc + my_off +
-                                                   static_cast<int64_t>(r) * p.bs;
+            int r2 = my_m2 - rho % p.nb;
+            if (r2 < 0) r2 += p.nb;
+            const int64_t rowb = step * p.t_step_stride + static_cast<int64_t>(rho) * p.spc;
+            const int64_t off_l = my_off < 0 ? -1 : rowb + my_off + static_cast<int64_t>(r) * p.bs;
+            const int64_t off_l2 = my_off2 < 0 ? -1 : rowb + my_off2 + static_cast<int64_t>(r2) * p.bs;
             const float isc = p.inv_scale[gu];
             bool ok = true;
             for (int h = 0; h < NH; ++h) {
@@ -338,19 +342,28 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
                 const bool jok = j < p.bs;
                 float2* base = p.T + j;
                 const uint32_t tb = tmem + (static_cast<uint32_t>(sp * 32) << 16) + h * 256 + cbase;
-#pragma unroll 1
-                for (int i = 0; i < 32; i += 16) {
-                    float re[16], im[16];
-                    tc_ld8(tb + i, re);
-                    tc_ld8(tb + i + 8, re + 8);
-                    tc_ld8(tb + 128 + i, im);
-                    tc_ld8(tb + 128 + i + 8, im + 8);
-                    tc_wait_ld();
+                float re[2][16], im[2][16];
+                tc_ld8(tb + 0, re[0]);
+                tc_ld8(tb + 8, re[0] + 8);
+                tc_ld8(tb + 128, im[0]);
+                tc_ld8(tb + 128 + 8, im[0] + 8);
+                tc_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 64; i += 16) {
+                    const int cb = (i >> 4) & 1;
+                    if (i + 16 < 64) {
+                        tc_ld8(tb + i + 16, re[cb ^ 1]);
+                        tc_ld8(tb + i + 24, re[cb ^ 1] + 8);
+                        tc_ld8(tb + 128 + i + 16, im[cb ^ 1]);
+                        tc_ld8(tb + 128 + i + 24, im[cb ^ 1] + 8);
+                    }
+                    const int64_t ol = i < 32 ? off_l : off_l2;
 #pragma unroll
                     for (int e = 0; e < 16; ++e) {
-                        const int64_t off = __shfl_sync(0xffffffffu, off_l, i + e);
-                        if (off >= 0 && jok) base[off] = make_float2(re[e] * isc, im[e] * isc);
+                        const int64_t off = __shfl_sync(0xffffffffu, ol, (i & 31) + e);
+                        if (off >= 0 && jok) __stcs(base + off, make_float2(re[cb][e] * isc, im[cb][e] * isc));
                     }
+                    tc_wait_ld();
                 }
                 tc_fence_before();
                 __syncwarp();
