@@ -590,10 +590,14 @@ void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
 
 // Tensor-core coherent tile (k_tile_mma): used on the TMA simple path when the block size fits
 // its operands (bs <= 256) and ACQ_OPT_TILE_MMA is on. The FP32 FFT tile stays the fallback.
+bool tile_mma_possible(const acq_plan* P) {
+    return P->tmma_enabled && P->g.bs <= kTmmaMaxBs && !getenv_flag("ACQ_NO_TILE_MMA");
+}
+
 void setup_tile_mma(acq_plan* P) {
     const Geometry& g = P->g;
     P->tmma = false;
-    if (!P->tmma_enabled || !P->col_tma || g.bs > kTmmaMaxBs || getenv_flag("ACQ_NO_TILE_MMA")) return;
+    if (!P->col_tma || !tile_mma_possible(P)) return;
     const int G = g.n_coh * g.nb;
     const size_t row_bytes = tmma_row_bytes(g.bs);
     // one CTA per SM: a CTA holds up to 512 tensor-memory columns
@@ -613,7 +617,12 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->col_tma = nullptr;
     P->col_pre = false;
     P->col_k1 = nullptr;
-    if (g.path != 0 || !P->tile_fs || getenv_flag("ACQ_GENERIC_FFT") || getenv_flag("ACQ_NO_TMA")) return;
+    P->tmma = false;
+    // the all-steps column stage needs an all-steps tile: the FFT tile's instantiation for the
+    // transform length, or the tensor-core tile (any length)
+    if (g.path != 0 || (!P->tile_fs && !tile_mma_possible(P)) || getenv_flag("ACQ_GENERIC_FFT") ||
+        getenv_flag("ACQ_NO_TMA"))
+        return;
     ColTmaFn fn = pick_col_tma(g.ndop);
     bool pre = false;
     if (g.n_coh <= 64 && !getenv_flag("ACQ_NO_PREPASS"))
@@ -681,6 +690,11 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->smem_col_tma = smem;
     if (pre) setup_col_k1(P, n_prns, P->k1W, P->k1CtasPerSm);
     setup_tile_mma(P);
+    if (!P->tmma && !P->tile_fs) {   // no tile for this stage: the per-step kernels
+        P->col_tma = nullptr;
+        P->col_pre = false;
+        P->col_k1 = nullptr;
+    }
 }
 
 void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
@@ -1930,7 +1944,7 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             if (value != 0 && value != 1) throw AcqError(ACQ_ERR_ARGUMENT, "tile MMA must be 0 or 1");
             CK(cudaStreamSynchronize(P->stream));
             P->tmma_enabled = value != 0;
-            setup_tile_mma(P);
+            setup_col_tma(P, P->n_plan_prns, P->tmaW, P->tmaCtasPerSm);   // calls setup_tile_mma
             if (effective) *effective = P->tmma ? 1 : 0;
             return;
         }

@@ -229,9 +229,10 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
         mbar_fence_init();
     }
     if (warp == 0) tc_alloc(tslot, tcols);
-    // B: code rows of this block, K-major, samples b >= bs zero
+    // B: code rows of this block, K-major, samples b >= bs zero (consecutive threads take
+    // consecutive rows: eight 16-byte rows of a core matrix fill all banks)
     for (int i = tid; i < kTmmaRows * KCH; i += kTmmaThreads) {
-        const int row = i / KCH, kc = i - row * KCH;
+        const int row = i % kTmmaRows, kc = i / kTmmaRows;
         const int gr = chunk * kTmmaRows + row;
         const int pi = gr / p.nb, m = gr - pi * p.nb;
         uint32_t w[4] = {0u, 0u, 0u, 0u};

@@ -56,6 +56,20 @@ def test_tile_mma_matches_the_fft_tile(quant):
     _compare(got, ref, quant)
 
 
+@pytest.mark.parametrize("fs", [2.5e6, 3.2e6])
+def test_tile_mma_block_sizes(fs):
+    # 2.5 MHz: block size 125 (odd; one lag half of 128, 8 K steps); 3.2 MHz: block size 200
+    # (two lag halves, 13 K steps)
+    sats = [synth.Satellite(6, 45.0, 700.0, 333.25)]
+    prns = [6, 7, 8]
+    plan = A.plan_acquire(A.GPSL1CA(), fs, prns, min_doppler_coverage=5000,
+                          num_coherently_integrated_code_periods=2, num_noncoherent_accumulations=2)
+    assert plan.geometry.block_size == {2.5e6: 125, 3.2e6: 200}[fs]
+    x = synth.to_ci16(synth.synth(A.GPSL1CA(), fs, 4 * plan.samples_per_code, sats, 3))
+    got, ref = _both(plan, x, prns)
+    _compare(got, ref, fs)
+
+
 def test_tile_mma_with_an_intermediate_frequency_and_one_coherent_period():
     # 4 MHz, 1 ms, IF 100 kHz: the operand kernel wipes the IF off per sample like the front end
     sats = [synth.Satellite(1, 45.0, 1234.0, 300.5)]
