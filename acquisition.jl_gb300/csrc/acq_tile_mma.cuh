@@ -296,16 +296,18 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
                     }
                     tc_commit(&full[h]);
                     ++n_full[h];
+                    // with half 0 of unit u queued behind them, the MMAs of unit u - 1 finish; the
+                    // next unit's operand blocks then go into their buffer and have the rest of
+                    // unit u's MMAs to land
+                    if (h == 0 && u >= 1 && u + 1 < nu) {
+                        const int bn = (u + 1) & 1;
+                        if (!(ok = tmma_wait(&sfree[bn], ((u - 1) >> 1) & 1, p.err, abort_flag))) break;
+                        prefetch(u + 1);
+                    }
                 }
                 if (!ok) break;
                 tc_commit(&sfree[b]);
                 ++n_free[b];
-                // buffer (u + 1) & 1 held unit u - 1, whose MMAs were issued before unit u's
-                if (u >= 1 && u + 1 < nu) {
-                    const int bn = (u + 1) & 1;
-                    if (!(ok = tmma_wait(&sfree[bn], ((u - 1) >> 1) & 1, p.err, abort_flag))) break;
-                    prefetch(u + 1);
-                }
             }
             if (!ok) {
                 // let every copy and MMA still in flight land before the block's memory is released
