@@ -180,6 +180,22 @@ def test_e1b_boc_12mhz():
     _compare(res, outs, "e1b-12mhz")
 
 
+def test_e1b_boc_2_5mhz_tensor_core_tile():
+    # block size 200 (no FFT-tile instantiation for the 400-point transform): the coherent tile is
+    # the tensor-core correlation GEMM, with BOC code samples
+    sats = [synth.Satellite(19, 46.0, -1800.0, 1500.75, data_bits=False)]
+    plan, res, outs = _run_case("GalileoE1B", 2.5e6, [19, 20, 21], cov=5000, sats=sats, seed=13)
+    assert plan.geometry.block_size == 200 and plan.get_option(11) == 1
+    _compare(res, outs, "e1b-2.5mhz-mma")
+
+
+def test_l5i_5mhz_tensor_core_tile_ci8():
+    sats = [synth.Satellite(7, 47.0, 3300.0, 9000.5, data_bits=False)]
+    plan, res, outs = _run_case("GPSL5I", 5e6, [7, 8], cov=5000, sats=sats, seed=17, quant="ci8")
+    assert plan.geometry.block_size == 250 and plan.get_option(11) == 1
+    _compare(res, outs, "l5i-5mhz-mma")
+
+
 def test_opt_out_golden_vector_on_gpu():
     # test/secondary_code_search.jl:119-130 through the CUDA path
     fs = 10.24e6
