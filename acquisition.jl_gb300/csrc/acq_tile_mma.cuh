@@ -21,7 +21,7 @@
 // n_coh-point DFT of k_doppler_prepass, applied to the time-domain blocks: the map is linear and
 // acts on rows only). k_tile_mma keeps one 128-row block of code rows resident per CTA and loops
 // over rows g: a bulk copy brings the row's Q_s, one thread issues the MMAs into tensor memory,
-// and all warps move D (times the row's inverse scale) to the tile with tcgen05.ld.
+// and the drain warps move D (times the row's inverse scale) to the tile with tcgen05.ld.
 #pragma once
 
 #include "acq_mma.cuh"
@@ -171,7 +171,7 @@ __host__ __device__ constexpr int tmma_smem_bytes(int bs) {
 }
 
 // Bounded mbarrier wait that also gives up when another warp has recorded an error (polled
-// every 256 tries); on its own timeout it records `code` and raises the block's abort flag.
+// every 256 tries); on its own timeout it records error 6 and raises the block's abort flag.
 __device__ __forceinline__ bool tmma_wait(uint64_t* bar, uint32_t parity, int* err, volatile int* abort_flag) {
     for (uint32_t i = 0; i < kWaitLimit; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
