@@ -588,16 +588,19 @@ void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
     P->smem_col_k1 = smem;
 }
 
-// Tensor-core coherent tile (k_tile_mma): used on the TMA simple path when the block size fits
-// its operands (bs <= 256) and ACQ_OPT_TILE_MMA is on. The FP32 FFT tile stays the fallback.
+// Tensor-core coherent tile (k_tile_mma): used when the block size fits its operands
+// (bs <= 256) and ACQ_OPT_TILE_MMA is on, for all steps in one launch on the TMA simple path and
+// one launch per step on the others. The FP32 FFT tiles stay the fallback (and ACQ_GENERIC_FFT
+// keeps the generic kernels).
 bool tile_mma_possible(const acq_plan* P) {
-    return P->tmma_enabled && P->g.bs <= kTmmaMaxBs && !getenv_flag("ACQ_NO_TILE_MMA");
+    return P->tmma_enabled && P->g.bs <= kTmmaMaxBs && !getenv_flag("ACQ_NO_TILE_MMA") &&
+           !getenv_flag("ACQ_GENERIC_FFT");
 }
 
 void setup_tile_mma(acq_plan* P) {
     const Geometry& g = P->g;
     P->tmma = false;
-    if (!P->col_tma || !tile_mma_possible(P)) return;
+    if (!tile_mma_possible(P)) return;
     const int G = g.n_coh * g.nb;
     const size_t row_bytes = tmma_row_bytes(g.bs);
     // one CTA per SM: a CTA holds up to 512 tensor-memory columns
@@ -607,6 +610,10 @@ void setup_tile_mma(acq_plan* P) {
     P->invsc.ensure(sizeof(float) * g.n_nc * G);
     set_smem((const void*)k_tile_mma, smem);
     CK(cudaDeviceGetAttribute(&P->tmmaSms, cudaDevAttrMultiProcessorCount, P->device));
+    if (!P->errflag.p) {
+        P->errflag.ensure(sizeof(int));
+        CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
+    }
     P->smem_tmma = smem;
     P->tmma = true;
 }
@@ -617,7 +624,6 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->col_tma = nullptr;
     P->col_pre = false;
     P->col_k1 = nullptr;
-    P->tmma = false;
     // the all-steps column stage needs an all-steps tile: the FFT tile's instantiation for the
     // transform length, or the tensor-core tile (any length)
     if (g.path != 0 || (!P->tile_fs && !tile_mma_possible(P)) || getenv_flag("ACQ_GENERIC_FFT") ||
@@ -689,8 +695,7 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     P->tmaH = H;
     P->smem_col_tma = smem;
     if (pre) setup_col_k1(P, n_prns, P->k1W, P->k1CtasPerSm);
-    setup_tile_mma(P);
-    if (!P->tmma && !P->tile_fs) {   // no tile for this stage: the per-step kernels
+    if (!tile_mma_possible(P) && !P->tile_fs) {   // no tile for this stage: the per-step kernels
         P->col_tma = nullptr;
         P->col_pre = false;
         P->col_k1 = nullptr;
@@ -813,6 +818,7 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
     setup_fused(P);
     P->n_plan_prns = n_prns;
     setup_col_tma(P, n_prns);
+    setup_tile_mma(P);
     {
         std::vector<int32_t> perm(g.spc_eff);
         chip_order(g.nb, g.bs, g.spc_eff, P->sys->code_freq, P->desc.sampling_freq_hz, perm.data(), nullptr);
@@ -959,9 +965,11 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     const int G = g.n_coh * g.nb;
     const bool use_fused = P->fused && P->form == ACQ_FORM_FUSED;
     const bool use_tma = !use_fused && P->col_tma != nullptr && P->dft_mma == nullptr;
-    // the tensor-core tile reads the samples itself: no block spectra
+    // the tensor-core tile reads the samples itself: no block spectra (all steps in one launch on
+    // the TMA path, one launch per step otherwise)
     const bool use_tmma = use_tma && P->tmma;
-    if (!use_tmma) {
+    const bool use_tmma_step = !use_fused && !use_tma && P->tmma;
+    if (!use_tmma && !use_tmma_step) {
         t_begin(P, ACQ_KERNEL_FRONTEND);
         k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF,
                                                                 P->S.as<float2>(), use_if, if_step, a.d_if_off);
@@ -1080,10 +1088,30 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             ++L;
         }
     }
+    if (use_tmma_step) {
+        t_begin(P, ACQ_KERNEL_FRONTEND);
+        k_tile_stubs<<<dim3(G, g.n_nc), kTmmaStubThreads, 0, st>>>(
+            d_in, dtype, seg_len, G, g.nb, g.n_coh, g.bs, 0, use_if, if_step, a.d_if_off, P->fftD.tw,
+            P->stubs.as<uint8_t>(), P->invsc.as<float>());
+        t_end(P);
+        ++L;
+    }
     for (int m = 0; m < ((use_fused || use_tma) ? 0 : g.n_nc); ++m) {
         const float2* Sm = P->S.as<float2>() + (size_t)m * G * g.fft_tile;
         t_begin(P, ACQ_KERNEL_TILE);
-        if (P->tile_fs)
+        if (use_tmma_step) {
+            TileMmaParams tp{};
+            const size_t row_bytes = tmma_row_bytes(g.bs);
+            tp.stubs = P->stubs.as<uint8_t>() + (size_t)m * G * row_bytes;
+            tp.inv_scale = P->invsc.as<float>() + (size_t)m * G;
+            tp.codes = P->codes.as<int8_t>(); tp.slots = a.d_slots; tp.T = P->T.as<float2>(); tp.t_step_stride = 0;
+            tp.n = n; tp.G = G; tp.nb = g.nb; tp.bs = g.bs; tp.spc = g.spc;
+            tp.n_chunks = (n * g.nb + kTmmaRows - 1) / kTmmaRows;
+            tp.units = G;
+            tp.cpc = std::max(1, std::min(tp.units, P->tmmaSms / tp.n_chunks));
+            tp.err = P->errflag.as<int>();
+            k_tile_mma<<<tp.n_chunks * tp.cpc, kTmmaThreads, P->smem_tmma, st>>>(tp);
+        } else if (P->tile_fs)
             P->tile_fs<<<dim3(tile_grid_x(P), n), P->tileThreads, P->smem_tile_fs, st>>>(
                 Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
                 P->T.as<float2>(), 0, P->tileFS);
@@ -1944,7 +1972,8 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             if (value != 0 && value != 1) throw AcqError(ACQ_ERR_ARGUMENT, "tile MMA must be 0 or 1");
             CK(cudaStreamSynchronize(P->stream));
             P->tmma_enabled = value != 0;
-            setup_col_tma(P, P->n_plan_prns, P->tmaW, P->tmaCtasPerSm);   // calls setup_tile_mma
+            setup_col_tma(P, P->n_plan_prns, P->tmaW, P->tmaCtasPerSm);
+            setup_tile_mma(P);
             if (effective) *effective = P->tmma ? 1 : 0;
             return;
         }

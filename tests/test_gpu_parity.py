@@ -196,6 +196,14 @@ def test_l5i_5mhz_tensor_core_tile_ci8():
     _compare(res, outs, "l5i-5mhz-mma")
 
 
+def test_l5i_rotation_5mhz_tensor_core_tile():
+    # the rotation search on tiles from the tensor-core GEMM (one launch per step)
+    sats = [synth.Satellite(9, 46.0, -2100.0, 4321.25)]
+    plan, res, outs = _run_case("GPSL5I", 5e6, [9, 10], n_coh=10, n_nc=2, cov=5000, sats=sats, seed=23, quant="ci8")
+    assert plan.geometry.path == 2 and plan.get_option(11) == 1
+    _compare(res, outs, "l5i-rot-5mhz-mma")
+
+
 def test_opt_out_golden_vector_on_gpu():
     # test/secondary_code_search.jl:119-130 through the CUDA path
     fs = 10.24e6

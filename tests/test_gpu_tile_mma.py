@@ -106,6 +106,30 @@ def test_tile_mma_many_prns_and_a_subset():
     _compare(got, ref, "subset")
 
 
+def test_tile_mma_per_step_for_the_bit_edge_search():
+    # data-bit / bit-edge search (40 ms, 2 data bits, 4 edges): one tile launch per step
+    sats = [synth.Satellite(5, 44.0, 1200.0, 512.5)]
+    prns = [5, 6, 7]
+    plan = A.plan_acquire(A.GPSL1CA(), 5e6, prns, min_doppler_coverage=5000,
+                          num_coherently_integrated_code_periods=40, bit_edge_search_steps=4)
+    assert plan.geometry.path == 1
+    x = synth.to_ci16(synth.synth(A.GPSL1CA(), 5e6, 40 * 5000, sats, 21))
+    got, ref = _both(plan, x, prns)
+    _compare(got, ref, "bit-edge")
+
+
+def test_tile_mma_per_step_for_the_rotation_search():
+    # secondary-code rotation search (L5I 5 MHz, 10 ms x 2, CI8): one tile launch per step
+    sats = [synth.Satellite(7, 47.0, 3300.0, 9000.5)]
+    prns = [7, 8]
+    plan = A.plan_acquire(A.GPSL5I(), 5e6, prns, min_doppler_coverage=5000,
+                          num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=2)
+    assert plan.geometry.path == 2
+    x = synth.to_ci8_3bit(synth.synth(A.GPSL5I(), 5e6, 2 * 10 * 5000, sats, 22))
+    got, ref = _both(plan, x, prns)
+    _compare(got, ref, "rotation")
+
+
 def test_tile_mma_against_the_fp64_oracle():
     sats = [synth.Satellite(3, 43.0, 1500.0, 200.25)]
     prns = [3, 4]
