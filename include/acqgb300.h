@@ -184,9 +184,9 @@ int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 #define ACQ_OPT_TILE_ROWS 9          /* coherent-tile kernel: rows sharing g mod num_blocks per CTA (1 or 2) */
 #define ACQ_OPT_TRANSFORM_LENGTH 10  /* read-only: length of the block and tile transforms (>= 2 block_size;
                                         fft_size, or a power of two or five times one up to 5 % longer) */
-#define ACQ_OPT_TILE_MMA 11          /* simple path, block_size <= 256: the coherent tile as a time-domain
-                                        correlation GEMM on the tensor cores (FP16 codes x FP16 hi + lo samples,
-                                        FP32 accumulation) = 1 (default where available), FP32 FFTs = 0 */
+#define ACQ_OPT_TILE_MMA 11          /* block_size <= 256: the coherent tile as a time-domain correlation GEMM
+                                        on the tensor cores (FP16 codes x FP16 hi + lo samples, FP32
+                                        accumulation) = 1 (default where available), FP32 FFTs = 0 */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
  * form is used only where the plan's sizes have a fused kernel (otherwise plain).
