@@ -63,8 +63,10 @@ __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __r
     const float off = use_if ? if_offset[step] : 0.f;
     const int k = rho % nb, k1 = rho / nb;
     const int span = tmma_span(bs);
+    // g < G and t < 2 bs, so g bs + t < seg_len + bs: one subtraction wraps it
     auto sample = [&](int g, int t) -> float2 {
-        const int64_t pos = (static_cast<int64_t>(g) * bs + t) % seg_len;
+        int64_t pos = static_cast<int64_t>(g) * bs + t;
+        if (pos >= seg_len) pos -= seg_len;
         float2 v = load_sample(in, dtype, seg0 + pos);
         if (use_if) {
             const float ph = __fadd_rn(off, __fmul_rn(__ll2float_rn(pos), if_step));
