@@ -28,3 +28,39 @@ def test_cache_round_trip(tmp_path):
     (tmp_path / "bad.json").write_text("{not json")
     assert T.load_cache(str(tmp_path / "bad.json")) == {}
     json.loads(open(p).read())
+
+
+class _FakePlan:
+    """Records set_option calls; every option is accepted as given."""
+
+    def __init__(self):
+        self.calls = []
+
+    def set_option(self, opt, value):
+        self.calls.append((opt, value))
+        return value
+
+    def set_form(self, form):
+        return form
+
+
+def test_apply_passes_zero_only_for_knobs_where_zero_is_a_setting():
+    # tile_mma = 0 selects the FP32 FFT tile; a zero launch shape means "the plan lacks that kernel"
+    plan = _FakePlan()
+    eff = T.apply(plan, {"tile_mma": 0, "tile_threads": 0, "column_width": 64})
+    assert (T.KNOBS["tile_mma"], 0) in plan.calls
+    assert (T.KNOBS["column_width"], 64) in plan.calls
+    assert all(opt != T.KNOBS["tile_threads"] for opt, _ in plan.calls)
+    assert eff == {"tile_mma": 0, "column_width": 64}
+
+
+def test_tile_mma_is_a_candidate_knob():
+    class G:
+        num_blocks = 20
+        num_coherently_integrated_code_periods = 10
+
+    class P:
+        geometry = G()
+
+    cands = T.candidates(P())
+    assert cands["tile_mma"] == [1, 0]
