@@ -84,7 +84,7 @@ EXPORTED = ["acq_plan_desc_init", "acq_plan_query", "acq_plan_create", "acq_plan
             "acq_batch_fetch", "acq_batch_run", "acq_batch_stream", "acq_batch_launch_count",
             "acq_corr_create", "acq_corr_destroy", "acq_corr_eval", "acq_corr_vjp_samples", "acq_corr_refine",
             "acq_plan_get_option", "acq_chip_order", "acq_sort_power_bins_by_chip", "acq_gen_code_device",
-            "acq_selftest_bounded_wait", "acq_synth_signal"]
+            "acq_selftest_bounded_wait", "acq_synth_signal", "acq_plan_last_kernels"]
 ACQ_OPT_FORM = 0
 ACQ_OPT_ROTATION_PRECISION = 1
 ACQ_OPT_MMA_SCALE_LOG2 = 2
@@ -126,6 +126,7 @@ def load():
     lib.acq_fetch_results.argtypes = [P, C.POINTER(Result), C.POINTER(C.c_float)]
     lib.acq_plan_stream.argtypes = [P, C.POINTER(P)]
     lib.acq_plan_last_launch_count.argtypes = [P, C.POINTER(C.c_int64)]
+    lib.acq_plan_last_kernels.argtypes = [P, C.c_char_p, C.c_size_t]
     lib.acq_cfar_threshold.argtypes = [C.c_double, C.c_int64, C.c_int32, C.POINTER(C.c_double)]
     lib.acq_gen_code.argtypes = [C.c_int32, C.c_int32, C.c_int64, C.c_double, C.c_double, C.c_double,
                                  C.POINTER(C.c_int8)]

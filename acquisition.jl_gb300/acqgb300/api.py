@@ -232,6 +232,12 @@ class AcquisitionPlan:
         _check(L.load().acq_plan_last_launch_count(self._h, C.byref(n)))
         return n.value
 
+    def last_kernels(self) -> list:
+        """Names of the kernels the last acquisition launched, in order (acq_plan_last_kernels)."""
+        buf = C.create_string_buffer(8192)
+        _check(L.load().acq_plan_last_kernels(self._h, buf, len(buf)))
+        return [k for k in buf.value.decode().split(",") if k]
+
     def set_form(self, form: str) -> str:
         """'plain' (one kernel per stage, the default) or 'fused' (cluster kernel where supported).
         Returns the form in effect."""

@@ -14,6 +14,16 @@
 
 namespace acq {
 
+// Names of the size-specialised kernels, for the launch log of acq_plan_last_kernels: each
+// picker records the name of the instantiation it returns.
+void note_kernel_name(const void* fn, const char* name);
+const char* kernel_name(const void* fn);
+template <class F>
+inline F named(F fn, const char* name) {
+    note_kernel_name(reinterpret_cast<const void*>(fn), name);
+    return fn;
+}
+
 using TileFsFn = void (*)(const float2*, const float2*, const int*, int, int, int, int, const float2*, int, float2*,
                           int64_t, int);
 using FusedFn = void (*)(FusedParams);

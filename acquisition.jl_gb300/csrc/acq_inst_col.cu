@@ -4,11 +4,11 @@
 namespace acq {
 
 #define ACQ_COL_CASE(N) \
-    case N: return &k_col_simple_fs<best_split_n1(N), N / best_split_n1(N)>;
+    case N: return named(&k_col_simple_fs<best_split_n1(N), N / best_split_n1(N)>, "k_col_simple_fs<" #N ">");
 #define ACQ_COLTMA_CASE(N) \
-    case N: return &k_col_tma<best_split_n1(N), N / best_split_n1(N), false>;
+    case N: return named(&k_col_tma<best_split_n1(N), N / best_split_n1(N), false>, "k_col_tma<" #N ">");
 #define ACQ_COLTMA_PRE_CASE(N) \
-    case N: return &k_col_tma<1, N, true>;
+    case N: return named(&k_col_tma<1, N, true>, "k_col_tma_pre<" #N ">");
 
 ColFsFn pick_col_fs(int ndop) {
     switch (ndop) {
@@ -21,15 +21,15 @@ ColFsFn pick_col_fs(int ndop) {
 
 ColTmaFn pick_col_tma_k1(int nb) {
     switch (nb) {
-        case 8: return &k_col_tma_k1<8>;
-        case 10: return &k_col_tma_k1<10>;
-        case 16: return &k_col_tma_k1<16>;
-        case 20: return &k_col_tma_k1<20>;
-        case 25: return &k_col_tma_k1<25>;
-        case 32: return &k_col_tma_k1<32>;
-        case 40: return &k_col_tma_k1<40>;
-        case 50: return &k_col_tma_k1<50>;
-        case 64: return &k_col_tma_k1<64>;
+        case 8: return named(&k_col_tma_k1<8>, "k_col_tma_k1<8>");
+        case 10: return named(&k_col_tma_k1<10>, "k_col_tma_k1<10>");
+        case 16: return named(&k_col_tma_k1<16>, "k_col_tma_k1<16>");
+        case 20: return named(&k_col_tma_k1<20>, "k_col_tma_k1<20>");
+        case 25: return named(&k_col_tma_k1<25>, "k_col_tma_k1<25>");
+        case 32: return named(&k_col_tma_k1<32>, "k_col_tma_k1<32>");
+        case 40: return named(&k_col_tma_k1<40>, "k_col_tma_k1<40>");
+        case 50: return named(&k_col_tma_k1<50>, "k_col_tma_k1<50>");
+        case 64: return named(&k_col_tma_k1<64>, "k_col_tma_k1<64>");
         default: return nullptr;
     }
 }

@@ -7,20 +7,26 @@ namespace acq {
 
 namespace {
 template <int NC, int NB, int QP, int CB>
-RotMmaFn pick_prec(int prec, size_t* smem) {
+RotMmaFn pick_prec(int prec, size_t* smem, const char* const name[4]) {
     using S = RotMmaShape<NC, NB, QP>;
     switch (prec) {
-        case ACQ_PREC_FP16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, CB, 0, 1>;
-        case ACQ_PREC_BF16: *smem = S::smem_bytes(1); return &k_rot_mma<NC, NB, QP, CB, 1, 1>;
-        case ACQ_PREC_FP16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, CB, 0, 2>;
-        case ACQ_PREC_BF16_SPLIT: *smem = S::smem_bytes(2); return &k_rot_mma<NC, NB, QP, CB, 1, 2>;
+        case ACQ_PREC_FP16: *smem = S::smem_bytes(1); return named(&k_rot_mma<NC, NB, QP, CB, 0, 1>, name[0]);
+        case ACQ_PREC_BF16: *smem = S::smem_bytes(1); return named(&k_rot_mma<NC, NB, QP, CB, 1, 1>, name[1]);
+        case ACQ_PREC_FP16_SPLIT: *smem = S::smem_bytes(2); return named(&k_rot_mma<NC, NB, QP, CB, 0, 2>, name[2]);
+        case ACQ_PREC_BF16_SPLIT: *smem = S::smem_bytes(2); return named(&k_rot_mma<NC, NB, QP, CB, 1, 2>, name[3]);
         default: return nullptr;
     }
 }
 }  // namespace
 
-#define ACQ_MMA_CASE(NC, NB, QP, CB) \
-    if (n_coh == NC && nb == NB && qp == QP && combos == CB) return pick_prec<NC, NB, QP, CB>(prec, smem);
+#define ACQ_MMA_NAME(NC, NB, QP, CB, F, S) "k_rot_mma<" #NC "," #NB "," #QP "," #CB "," F "," S ">"
+#define ACQ_MMA_CASE(NC, NB, QP, CB)                                                                      \
+    if (n_coh == NC && nb == NB && qp == QP && combos == CB) {                                           \
+        static const char* const name[4] = {                                                            \
+            ACQ_MMA_NAME(NC, NB, QP, CB, "fp16", "1"), ACQ_MMA_NAME(NC, NB, QP, CB, "bf16", "1"),        \
+            ACQ_MMA_NAME(NC, NB, QP, CB, "fp16", "2"), ACQ_MMA_NAME(NC, NB, QP, CB, "bf16", "2")};       \
+        return pick_prec<NC, NB, QP, CB>(prec, smem, name);                                              \
+    }
 
 RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec, size_t* smem) {
     const int qp = (n_candidates + 7) / 8 * 8;

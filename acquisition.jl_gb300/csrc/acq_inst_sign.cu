@@ -4,9 +4,9 @@
 namespace acq {
 
 #define ACQ_SIGN_CASE(N) \
-    case N: return &k_col_sign_fs<best_split_n1(N), N / best_split_n1(N)>;
+    case N: return named(&k_col_sign_fs<best_split_n1(N), N / best_split_n1(N)>, "k_col_sign_fs<" #N ">");
 #define ACQ_ROT_CASE(N) \
-    case N: return &k_col_rot_fs<best_split_n1(N), N / best_split_n1(N)>;
+    case N: return named(&k_col_rot_fs<best_split_n1(N), N / best_split_n1(N)>, "k_col_rot_fs<" #N ">");
 
 SignFsFn pick_sign_fs(int ndop) {
     switch (ndop) {
@@ -29,7 +29,9 @@ RotFsFn pick_rot_fs(int ndop) {
         constexpr int kW = (NC * NB <= 384) ? 16 : 8;                       \
         *w = kW;                                                            \
         *threads = rot_sb_block(NC, NB, kW);                                \
-        return &k_col_rot_sb<NC, NB, kW>;                                   \
+        return named(&k_col_rot_sb<NC, NB, kW>,                             \
+                     kW == 16 ? "k_col_rot_sb<" #NC "," #NB ",16>"          \
+                              : "k_col_rot_sb<" #NC "," #NB ",8>");         \
     }
 
 RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
@@ -43,7 +45,8 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
         *w = W;                                                                                      \
         *threads = (1 << (NDB - 1)) * N1 * W;                                                         \
         *smem = sizeof(float2) * ((size_t)(1 + NDB) * N1 * N2 * W + N1 * N2) + 64;                    \
-        return &k_col_sign_sb<N1, N2, W, NDB>;                                                        \
+        return named(&k_col_sign_sb<N1, N2, W, NDB>,                                                  \
+                     "k_col_sign_sb<" #N1 "," #N2 "," #W "," #NDB ">");                              \
     }
 
 SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {

@@ -5,8 +5,8 @@ namespace acq {
 
 #define ACQ_TILE_CASE(F)                                                                     \
     case F:                                                                                  \
-        return rows == 2 ? &k_tile_fs<best_split_n1(F), F / best_split_n1(F), 2>             \
-                         : &k_tile_fs<best_split_n1(F), F / best_split_n1(F), 1>;
+        return rows == 2 ? named(&k_tile_fs<best_split_n1(F), F / best_split_n1(F), 2>, "k_tile_fs<" #F ",2>") \
+                         : named(&k_tile_fs<best_split_n1(F), F / best_split_n1(F), 1>, "k_tile_fs<" #F ",1>");
 
 TileFsFn pick_tile_fs(int F, int rows) {
     if (rows != 1 && rows != 2) return nullptr;
@@ -20,7 +20,8 @@ TileFsFn pick_tile_fs(int F, int rows) {
 
 #define ACQ_FUSED_CASE(F, D) \
     if (fft == F && ndop == D)   \
-        return &k_fused_simple<best_split_n1(F), F / best_split_n1(F), best_split_n1(D), D / best_split_n1(D)>;
+        return named(&k_fused_simple<best_split_n1(F), F / best_split_n1(F), best_split_n1(D), D / best_split_n1(D)>, \
+                     "k_fused_simple<" #F "," #D ">");
 
 FusedFn pick_fused(int fft, int ndop) {
     // transform lengths as chosen by the runtime (powers of two, or five times one, where possible)

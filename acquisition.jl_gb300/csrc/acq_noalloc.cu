@@ -13,13 +13,13 @@
 //  - All calls on a device share the one scratch array. Each call clears the part it uses
 //    before the reduction, so nothing carries over between calls, but calls that overlap on
 //    the GPU (different streams, or host threads without ordering) race on it: order them.
-//  - The first call on each device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current) and caches it; make that first call
-//    before any stream capture.
+//  - Every call looks up the array's device address for the current device with
+//    cudaGetSymbolAddress (nothing is cached, so a device reset between calls leaves no stale
+//    address behind). The first call on a device may load this library's device code there;
+//    make that first call before any stream capture.
 //  - Nothing here calls cudaMalloc, cudaFree or an allocating library routine.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "acq_host.h"
@@ -30,14 +30,10 @@ namespace {
 constexpr int kNoAllocMaxDopplerBins = 4096;
 constexpr int kNoAllocHeaderWords = 4;   // [0] peak key, [1] total (double), [2] exclusion sum (double)
 constexpr int kNoAllocWords = kNoAllocHeaderWords + kNoAllocMaxDopplerBins;
-constexpr int kMaxDevices = 64;
 constexpr int kCols = 256;
 
 // 32 KiB + 32 B of scratch: the peak key, two FP64 sums and one FP64 sum per Doppler row.
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocWords];
-
-std::mutex g_mu;
-unsigned long long* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 __device__ __forceinline__ unsigned long long nk(float v, uint32_t order) {
     return (static_cast<unsigned long long>(__float_as_uint(v)) << 32) |
@@ -166,22 +162,11 @@ extern "C" int acq_est_signal_noise_power_noalloc(const float* d_power_bins, int
         return fail(ACQ_ERR_ARGUMENT, "unknown noise estimator " + std::to_string(noise_estimator));
     if (!(sampling_freq_hz > 0) || !(code_freq_hz > 0))
         return fail(ACQ_ERR_ARGUMENT, "sampling and code frequencies must be positive");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(ACQ_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(ACQ_ERR_UNSUPPORTED, "device ordinal out of range");
-    unsigned long long* scratch;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_scratch_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess)
-                return fail(ACQ_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_scratch_ptr[dev] = static_cast<unsigned long long*>(p);
-        }
-        scratch = g_scratch_ptr[dev];
-    }
+    // the scratch array's address on the current device, looked up on every call
+    void* sp = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&sp, g_noalloc_scratch);
+    if (e != cudaSuccess) return fail(ACQ_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    unsigned long long* scratch = static_cast<unsigned long long*>(sp);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t clear = sizeof(unsigned long long) * (kNoAllocHeaderWords + num_doppler_bins);
     e = cudaMemsetAsync(scratch, 0, clear, st);

@@ -11,7 +11,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "acq_host.h"
@@ -21,6 +23,25 @@
 #include "acq_tile_mma.cuh"
 
 using namespace acq;
+
+namespace {
+std::mutex g_name_mu;
+std::unordered_map<const void*, const char*>& name_table() {
+    static std::unordered_map<const void*, const char*> t;
+    return t;
+}
+}  // namespace
+
+void acq::note_kernel_name(const void* fn, const char* name) {
+    std::lock_guard<std::mutex> lk(g_name_mu);
+    name_table()[fn] = name;
+}
+
+const char* acq::kernel_name(const void* fn) {
+    std::lock_guard<std::mutex> lk(g_name_mu);
+    auto it = name_table().find(fn);
+    return it == name_table().end() ? nullptr : it->second;
+}
 
 namespace {
 
@@ -384,6 +405,7 @@ struct acq_plan {
     int fusedCL = 8, fusedRPC = 1, fusedCPC = 1, fusedNF = 1, fusedH = 0;
     size_t smem_fused = 0;
     // last acquisition
+    std::vector<std::string> klog;   // kernels of the last launch sequence, in launch order
     int last_n = 0;
     uint32_t last_flags = 0;
     int64_t launches = 0;
@@ -426,6 +448,12 @@ void t_end(acq_plan* P) {
     if (!P->timing) return;
     CK(cudaEventRecord(P->ev_stop[P->ev_used], P->stream));
     ++P->ev_used;
+}
+
+// Launch log: the kernel about to be launched (a size-specialised kernel by its registered name).
+void klog(acq_plan* P, const void* fn, const char* fallback) {
+    const char* nm = fn ? kernel_name(fn) : nullptr;
+    P->klog.emplace_back(nm ? nm : fallback);
 }
 
 void t_collect(acq_plan* P) {
@@ -961,6 +989,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     const int use_if = a.use_if;
     const float if_step = a.if_step;
     int64_t L = 0;
+    P->klog.clear();
     int stats_nct = 0, stats_npk = 0;   // set when the column stage produced the statistics
     const int G = g.n_coh * g.nb;
     const bool use_fused = P->fused && P->form == ACQ_FORM_FUSED;
@@ -971,6 +1000,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     const bool use_tmma_step = !use_fused && !use_tma && P->tmma;
     if (!use_tmma && !use_tmma_step) {
         t_begin(P, ACQ_KERNEL_FRONTEND);
+        klog(P, nullptr, "k_frontend");
         k_frontend<<<g.n_nc * G, kThreads, P->smem_front, st>>>(d_in, dtype, seg_len, G, g.bs, P->fftF,
                                                                 P->S.as<float2>(), use_if, if_step, a.d_if_off);
         t_end(P);
@@ -997,6 +1027,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         t_begin(P, ACQ_KERNEL_FUSED);
+        klog(P, (const void*)P->fused, "k_fused_simple");
         CK(cudaLaunchKernelEx(&cfg, P->fused, fp));
         t_end(P);
         ++L;
@@ -1005,6 +1036,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         // operand blocks of every (step, row), then the correlation GEMM for all steps
         const int nprn = static_cast<int>(P->prns.size());
         t_begin(P, ACQ_KERNEL_FRONTEND);
+        klog(P, nullptr, "k_tile_stubs");
         k_tile_stubs<<<dim3(G, g.n_nc), kTmmaStubThreads, 0, st>>>(
             d_in, dtype, seg_len, G, g.nb, g.n_coh, g.bs, P->col_pre ? 1 : 0, use_if, if_step, a.d_if_off,
             P->fftD.tw, P->stubs.as<uint8_t>(), P->invsc.as<float>());
@@ -1019,6 +1051,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         tp.cpc = std::max(1, std::min(tp.units, P->tmmaSms / tp.n_chunks));
         tp.err = P->errflag.as<int>();
         t_begin(P, ACQ_KERNEL_TILE);
+        klog(P, nullptr, "k_tile_mma");
         k_tile_mma<<<tp.n_chunks * tp.cpc, kTmmaThreads, P->smem_tmma, st>>>(tp);
         t_end(P);
         ++L;
@@ -1029,6 +1062,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         const float2* spectra = P->S.as<float2>();
         if (!use_tmma && P->col_pre && g.n_coh > 1) {   // one coherent period: the first pass is the identity
             t_begin(P, ACQ_KERNEL_FRONTEND);
+            klog(P, nullptr, "k_doppler_prepass");
             k_doppler_prepass<<<dim3((g.fft_tile + 127) / 128, g.nb * g.n_coh, g.n_nc), 128, 0, st>>>(
                 P->S.as<float2>(), P->U.as<float2>(), G, g.nb, g.n_coh, g.fft_tile, P->fftD.tw);
             t_end(P);
@@ -1037,6 +1071,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         }
         if (!use_tmma) {
             t_begin(P, ACQ_KERNEL_TILE);
+            klog(P, (const void*)P->tile_fs, "k_tile_fs");
             P->tile_fs<<<dim3(tile_grid_x(P), n, g.n_nc), P->tileThreads, P->smem_tile_fs, st>>>(
                 spectra, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
                 P->Tall.as<float2>(), static_cast<int64_t>(nprn) * G * g.spc, P->tileFS);
@@ -1048,6 +1083,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             const int n_bound = (g.spc + wc - 1) / wc + 1;
             const int64_t rows = static_cast<int64_t>(n) * g.ndop;
             const int64_t total = rows * n_bound * 2 * P->tmaH;
+            klog(P, nullptr, "k_zero_edges");
             k_zero_edges<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
                 P->accb.as<float>(), rows, g.spc, g.spc_eff, wc, P->tmaH, n_bound);
             ++L;
@@ -1068,11 +1104,13 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             cp.peakpart = P->peakpart.as<unsigned long long>();
             cp.npk = g.n_coh * cp.n_cblk + (P->tmaH > 0 ? n_bound : 0);
             const int grid = std::max(1, std::min(P->k1Grid, cp.n_items));
+            klog(P, (const void*)P->col_k1, "k_col_tma_k1");
             P->col_k1<<<grid, 128, P->smem_col_k1, st>>>(P->tmapK1, cp);
             t_end(P);
             ++L;
             if (P->tmaH > 0) {
                 t_begin(P, ACQ_KERNEL_STATS);
+                klog(P, nullptr, "k_edge_peaks");
                 k_edge_peaks<<<dim3(n_bound, n), 128, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc, g.spc_eff, P->k1W,
                                                               P->tmaH, n_bound, g.n_coh * cp.n_cblk, cp.npk,
                                                               P->peakpart.as<unsigned long long>());
@@ -1083,6 +1121,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             stats_npk = cp.npk;
         } else {
             const int grid = std::max(1, std::min(P->tmaGrid, cp.n_items));
+            klog(P, (const void*)P->col_tma, "k_col_tma");
             P->col_tma<<<grid, kThreads, P->smem_col_tma, st>>>(P->tmapT, cp);
             t_end(P);
             ++L;
@@ -1090,6 +1129,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     }
     if (use_tmma_step) {
         t_begin(P, ACQ_KERNEL_FRONTEND);
+        klog(P, nullptr, "k_tile_stubs");
         k_tile_stubs<<<dim3(G, g.n_nc), kTmmaStubThreads, 0, st>>>(
             d_in, dtype, seg_len, G, g.nb, g.n_coh, g.bs, 0, use_if, if_step, a.d_if_off, P->fftD.tw,
             P->stubs.as<uint8_t>(), P->invsc.as<float>());
@@ -1110,14 +1150,18 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             tp.units = G;
             tp.cpc = std::max(1, std::min(tp.units, P->tmmaSms / tp.n_chunks));
             tp.err = P->errflag.as<int>();
+            klog(P, nullptr, "k_tile_mma");
             k_tile_mma<<<tp.n_chunks * tp.cpc, kTmmaThreads, P->smem_tmma, st>>>(tp);
-        } else if (P->tile_fs)
+        } else if (P->tile_fs) {
+            klog(P, (const void*)P->tile_fs, "k_tile_fs");
             P->tile_fs<<<dim3(tile_grid_x(P), n), P->tileThreads, P->smem_tile_fs, st>>>(
                 Sm, P->conj.as<float2>(), a.d_slots, G, g.nb, g.bs, g.spc, P->twT.as<float2>(), P->tileNF,
                 P->T.as<float2>(), 0, P->tileFS);
-        else
+        } else {
+            klog(P, nullptr, "k_tile");
             k_tile<<<dim3(G, n), kThreads, P->smem_tile, st>>>(Sm, P->conj.as<float2>(), a.d_slots, G, g.nb,
                                                                g.bs, g.spc, P->fftF, P->tileB, P->T.as<float2>());
+        }
         t_end(P);
         ++L;
         const int* dr = P->drift.as<int>() + (size_t)m * g.ndop;
@@ -1133,14 +1177,17 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             if (sl == 127) sl = dtype == ACQ_CI16 ? -10 : dtype == ACQ_CI8 ? -2 : 0;
             dp.scale = std::ldexp(1.0f, sl);
             dp.err = P->errflag.as<int>();
+            klog(P, (const void*)P->dft_mma, "k_col_dft_mma");
             P->dft_mma<<<dim3((g.spc + kDftCols - 1) / kDftCols, n), kDftThreads, P->smem_dft, st>>>(dp);
         } else if (g.path == 0 && P->col_fs) {
             const int W = P->Wfs;
+            klog(P, (const void*)P->col_fs, "k_col_simple_fs");
             P->col_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_col_fs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, dr, first, P->step_has_drift[m], P->accb.as<float>(),
                 g.spc_eff);
         } else if (g.path == 0) {
             const int W = P->Wsimple;
+            klog(P, nullptr, "k_col_simple");
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
         } else if (g.path == 2 && P->rot_mma) {
@@ -1153,21 +1200,25 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             if (sl == 127) sl = dtype == ACQ_CI16 ? -10 : dtype == ACQ_CI8 ? -2 : 0;
             rp.scale = std::ldexp(1.0f, sl);
             rp.err = P->errflag.as<int>();
+            klog(P, (const void*)P->rot_mma, "k_rot_mma");
             P->rot_mma<<<dim3((g.spc + kRotMmaW - 1) / kRotMmaW, n), 256, P->smem_mma, st>>>(rp);
         } else if (g.path == 2 && P->rot_sb) {
             const int W = P->Wrsb;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            klog(P, (const void*)P->rot_sb, "k_col_rot_sb");
             P->rot_sb<<<dim3((g.spc + W - 1) / W, n), P->threads_rsb, P->smem_rsb, st>>>(
                 P->T.as<float2>(), g.spc, P->fftD.tw, P->pats.as<float>(), g.bs, g.R, P->combos, g.n_be,
                 P->edge_step, use_max, a.d_slots, dr, first | (last ? 2 : 0), P->accb.as<float>(),
                 P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 1 && P->sign_sb) {
             const int W = P->Wssb;
+            klog(P, (const void*)P->sign_sb, "k_col_sign_sb");
             P->sign_sb<<<dim3((g.spc + W - 1) / W, n), P->threads_ssb, P->smem_ssb, st>>>(
                 P->T.as<float2>(), g.spc, P->fftD.tw, P->pats.as<float>(), g.n_coh, g.n_be, P->edge_step, a.d_slots,
                 dr, first | (last ? 2 : 0), P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 1 && P->sign_fs) {
             const int W = P->Wsfs;
+            klog(P, (const void*)P->sign_fs, "k_col_sign_fs");
             P->sign_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
                 P->edge_step, a.d_slots, dr, first | (last ? 2 : 0), P->accb.as<float>(), P->winb.as<uint16_t>(),
@@ -1175,18 +1226,21 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         } else if (g.path == 2 && P->rot_fs) {
             const int W = P->Wsfs;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            klog(P, (const void*)P->rot_fs, "k_col_rot_fs");
             P->rot_fs<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sfs, st>>>(
                 P->T.as<float2>(), g.spc, W, P->fftD.tw, P->pats.as<float>(), g.n_coh, g.nb, g.bs, g.R, P->combos,
                 g.n_be, P->edge_step, use_max, a.d_slots, dr, first, P->accb.as<float>(),
                 P->winb.as<uint16_t>(), g.spc_eff);
         } else if (g.path == 1) {
             const int W = P->Wsign;
+            klog(P, nullptr, "k_col_sign");
             k_col_sign<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, P->pats.as<float>(), P->n_pat, g.n_coh, g.ndb, g.n_be,
                 P->edge_step, a.d_slots, dr, first, P->accb.as<float>(), P->winb.as<uint16_t>(), g.spc_eff);
         } else {
             const int W = P->Wsign;
             const int use_max = (P->combos > 1 || g.n_be > 1) ? 1 : 0;
+            klog(P, nullptr, "k_col_rot");
             k_col_rot<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_sign, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, P->pats.as<float>(), g.n_coh, g.nb, g.bs, g.R, P->combos,
                 g.n_be, P->edge_step, use_max, a.d_slots, dr, first, P->accb.as<float>(),
@@ -1198,6 +1252,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     const int streamed_rot = (g.n_nc == 1 && g.R > 1) ? 1 : 0;
     if (stats_npk == 0) {
         t_begin(P, ACQ_KERNEL_STATS);
+        klog(P, nullptr, "k_stats");
         k_stats<<<dim3(P->nct, n), kThreads, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc_eff, g.spc, g.R, streamed_rot,
                                                       P->rowpart.as<double>(), P->colsum.as<double>(),
                                                       P->peakpart.as<unsigned long long>());
@@ -1218,6 +1273,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     EP.t_coh = g.n_coh * (static_cast<double>(P->sys->code_length) / P->sys->code_freq);
     EP.doppler_first = g.doppler_first; EP.doppler_step = g.doppler_step; EP.cfar_thr = g.cfar_thr;
     t_begin(P, ACQ_KERNEL_EXTRACT);
+    klog(P, nullptr, "k_extract");
     k_extract<<<n, kThreads, 0, st>>>(P->accb.as<float>(), P->winb.as<uint16_t>(), P->rowpart.as<double>(),
                                       P->colsum.as<double>(), P->peakpart.as<unsigned long long>(), a.d_prn_ids,
                                       EP, a.d_res);
@@ -1225,10 +1281,12 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     ++L;
     if (g.R > 1) {
         t_begin(P, ACQ_KERNEL_SECONDARY);
+        klog(P, nullptr, "k_secondary_prompt");
         k_secondary_prompt<<<dim3(n, g.R), kThreads, 0, st>>>(d_in, dtype, P->chips.as<int8_t>(), P->chips_len,
                                                               a.d_slots, g.spc, P->desc.sampling_freq_hz,
                                                               P->sys->code_freq, a.interm_freq, a.d_res,
                                                               P->zs.as<double2>(), g.R);
+        klog(P, nullptr, "k_secondary_argmax");
         k_secondary_argmax<<<(n + 127) / 128, 128, 0, st>>>(P->zs.as<double2>(), P->sec.as<int8_t>(), g.R,
                                                             a.d_res, n);
         t_end(P);
@@ -1688,6 +1746,19 @@ int acq_plan_last_launch_count(const acq_plan* P, int64_t* count) {
     });
 }
 
+int acq_plan_last_kernels(const acq_plan* P, char* buf, size_t len) {
+    return guarded([&] {
+        if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null plan");
+        std::string out;
+        for (size_t i = 0; i < P->klog.size(); ++i) out += (i ? "," : "") + P->klog[i];
+        if (buf && len) {
+            const size_t m = std::min(len - 1, out.size());
+            std::memcpy(buf, out.data(), m);
+            buf[m] = 0;
+        }
+    });
+}
+
 int acq_batch_create(const acq_batch_item* items, int32_t n_items, acq_batch** out) {
     return guarded([&] {
         if (!items || !out) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
@@ -1951,8 +2022,10 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
                     k_dft_operand<1><<<grid, 256, 0, P->stream>>>(g.ndop, npad, ksteps, nsplit, P->dftB.as<uint8_t>());
                 CK(cudaGetLastError());
                 CK(cudaStreamSynchronize(P->stream));
-                DftMmaFn fn = fmt == 0 ? (nsplit == 2 ? &k_col_dft_mma<0, 2> : &k_col_dft_mma<0, 1>)
-                                       : (nsplit == 2 ? &k_col_dft_mma<1, 2> : &k_col_dft_mma<1, 1>);
+                DftMmaFn fn = fmt == 0 ? (nsplit == 2 ? named(&k_col_dft_mma<0, 2>, "k_col_dft_mma<fp16,2>")
+                                                      : named(&k_col_dft_mma<0, 1>, "k_col_dft_mma<fp16,1>"))
+                                       : (nsplit == 2 ? named(&k_col_dft_mma<1, 2>, "k_col_dft_mma<bf16,2>")
+                                                      : named(&k_col_dft_mma<1, 1>, "k_col_dft_mma<bf16,1>"));
                 // one block per SM (the block holds 512 TMEM columns)
                 const size_t need = 1024 + 2 * (size_t)nsplit * 4096 + 2 * (size_t)nsplit * npad * 32 + 64;
                 const size_t smem = std::max<size_t>(need, 120 * 1024);

@@ -159,6 +159,13 @@ int acq_plan_stream(const acq_plan* plan, void** stream);
 /* Number of this library's kernel launches enqueued by the last acquisition. */
 int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 
+/* Names of this library's kernels launched by the last acquisition on the plan, in launch
+ * order, comma-separated; size-specialised kernels carry their template sizes, e.g.
+ * "k_tile_stubs,k_tile_mma,k_col_tma_k1<20>,k_extract". Written NUL-terminated to buf (truncated
+ * to len). A replayed CUDA graph reports the sequence it was captured from. Diagnostic, for
+ * tests that pin which instantiation a geometry runs; no reference counterpart. */
+int acq_plan_last_kernels(const acq_plan* plan, char* buf, size_t len);
+
 /* Plan options (acq_plan_set_option). */
 #define ACQ_OPT_FORM 0               /* ACQ_FORM_PLAIN (default) or ACQ_FORM_FUSED */
 #define ACQ_FORM_FUSED 0             /* cluster kernel: tile + Doppler stage + accumulation in shared memory */
@@ -332,8 +339,10 @@ typedef struct {
  * loads the library until exit), so num_doppler_bins is limited to 4096 and larger sizes
  * return ACQ_ERR_ARGUMENT. Asynchronous on `stream` (a cudaStream_t, NULL for the default
  * stream). Calls share the scratch and clear it themselves; calls that overlap on the GPU race
- * and must be ordered by the caller. The first call on a device resolves the scratch address
- * (cudaGetSymbolAddress); make it before any stream capture. */
+ * and must be ordered by the caller. Every call looks up the scratch address on the current
+ * device (cudaGetSymbolAddress, nothing cached, so a device reset between calls is safe); the
+ * first call on a device may load the library's device code there: make it before any stream
+ * capture. */
 int acq_est_signal_noise_power_noalloc(const float* d_power_bins, int32_t num_doppler_bins, int64_t num_code_bins,
                                        double sampling_freq_hz, double code_freq_hz, int32_t noise_estimator,
                                        acq_noise_stats* d_out, void* stream);

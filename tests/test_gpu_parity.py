@@ -308,3 +308,136 @@ def test_transform_lengths_and_doppler_groups(fs, n_coh, n_nc, cov, dop, nb, len
     assert plan.get_option(10) == length          # ACQ_OPT_TRANSFORM_LENGTH
     assert plan.get_option(6) == 128              # the Doppler-group column stage's default width
     _compare(res, outs, f"fs={fs} n_coh={n_coh} n_nc={n_nc} cov={cov}")
+
+
+# --------------------------------------------------------------------------------------------
+# The benchmarked workloads, at their exact instantiations, against the oracle. Each case pins
+# the kernels that ran (acq_plan_last_kernels) so that a change of dispatch cannot move the
+# benchmark onto a kernel these tests do not cover.
+# --------------------------------------------------------------------------------------------
+def _bench_input(config):
+    import bench
+    bench.set_config(config)
+    sig, sats = bench.make_input()
+    return bench, sig, sats
+
+
+def _oracles(name, fs, prns, osig, **kw):
+    _, o_sys = SYS[name]
+    outs = {}
+    for prec in ("f32", "f64"):
+        op = O.plan_acquire(o_sys, fs, prns, precision=prec, **kw)
+        outs[prec] = O.acquire_b(op, osig, prns, return_surfaces=True)
+    return outs
+
+
+def _complex(sig):
+    if np.iscomplexobj(sig):
+        return sig.astype(np.complex64)
+    return (sig[:, 0].astype(np.float32) + 1j * sig[:, 1].astype(np.float32)).astype(np.complex64)
+
+
+def test_headline_workload_exact_input_and_tuned_shapes():
+    # the 5 MHz, 10 ms x 8, +-5 kHz, 32-PRN CI16 workload with the benchmark's own input (seed
+    # 2024) and the launch shapes its autotuner settles on (128-column Doppler-group tiles, four
+    # column CTAs per SM)
+    from acqgb300 import _lib as L
+    bench, sig, sats = _bench_input("cfg2")
+    prns = list(range(1, 33))
+    kw = dict(min_doppler_coverage=5000.0, num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=8)
+    plan = A.plan_acquire(A.GPSL1CA(), 5e6, prns, **kw)
+    assert plan.set_option(L.ACQ_OPT_COLUMN_WIDTH, 128) == 128
+    assert plan.set_option(L.ACQ_OPT_COLUMN_CTAS_PER_SM, 4) == 4
+    res = A.acquire_b(plan, sig, prns, store_power_bins=True)
+    assert plan.last_kernels() == ["k_tile_stubs", "k_tile_mma", "k_zero_edges", "k_col_tma_k1<20>", "k_edge_peaks",
+                                   "k_extract"], plan.last_kernels()
+    outs = _oracles("GPSL1CA", 5e6, prns, _complex(sig), **kw)
+    _compare(res, outs, "headline-32prn")
+    # every detection decision (planted or not, false alarms included) equals the FP64 oracle's
+    det_gpu = [r.prn for r in res if A.is_detected(r)]
+    det_o64 = [r.prn for r in outs["f64"][0] if O.is_detected(r)]
+    det_o32 = [r.prn for r in outs["f32"][0] if O.is_detected(r)]
+    print(f"[headline] detected GPU {det_gpu}, FP64 oracle {det_o64}, FP32 oracle {det_o32}, "
+          f"planted {sorted(s.prn for s in sats)}")
+    assert det_gpu == det_o64 == det_o32
+
+
+def test_bit_edge_search_workload_geometry():
+    # 5 MHz, 40 ms x 2, four bit-edge steps (ndop 800, two data bits): the benchmark's input, on
+    # two of its planted satellites and one absent PRN
+    bench, sig, sats = _bench_input("cfg2b")
+    planted = sorted(s.prn for s in sats)
+    prns = planted[:2] + [p for p in range(1, 33) if p not in planted][:1]
+    kw = dict(min_doppler_coverage=5000.0, num_coherently_integrated_code_periods=40, num_noncoherent_accumulations=2,
+              bit_edge_search_steps=4)
+    plan = A.plan_acquire(A.GPSL1CA(), 5e6, prns, **kw)
+    assert plan.num_doppler_bins == 800 and plan.num_data_bits == 2
+    res = A.acquire_b(plan, sig, prns, store_power_bins=True)
+    ks = plan.last_kernels()
+    assert ks.count("k_col_sign_sb<32,25,8,2>") == 2, ks
+    _compare(res, _oracles("GPSL1CA", 5e6, prns, _complex(sig), **kw), "bit-edge-ndop800")
+
+
+@pytest.mark.parametrize("n_nc", [1, 2])
+def test_rotation_workload_geometry_all_precisions(n_nc):
+    # GPS L5I 20 MHz, 20 ms coherent, +-10 kHz, CI8 (nb 25, ndop 500, ten rotations x two
+    # data-bit combinations): the benchmark's input on its first n_nc accumulation steps, in
+    # FP32 and both split-precision tensor-core combines, against one oracle run
+    bench, sig, sats = _bench_input("cfg4")
+    planted = sorted(s.prn for s in sats)
+    prns = planted[:2] if n_nc == 2 else planted[2:3]
+    kw = dict(min_doppler_coverage=10000.0, num_coherently_integrated_code_periods=20, num_noncoherent_accumulations=n_nc)
+    n = n_nc * 20 * 20000
+    sig = sig[:n]
+    outs = _oracles("GPSL5I", 20e6, prns, _complex(sig), **kw)
+    plan = A.plan_acquire(A.GPSL5I(), 20e6, prns, **kw)
+    assert (plan.num_doppler_bins, plan.geometry.num_blocks, plan.num_secondary_rotations) == (500, 25, 10)
+    for prec, kernel in [("fp32", "k_col_rot_sb<20,25,8>"), ("fp16_split", "k_rot_mma<20,25,24,2,fp16,2>"),
+                         ("bf16_split", "k_rot_mma<20,25,24,2,bf16,2>")]:
+        assert plan.set_rotation_precision(prec) == prec
+        res = A.acquire_b(plan, sig, prns, store_power_bins=True)
+        ks = plan.last_kernels()
+        assert ks.count(kernel) == n_nc, ks
+        _compare(res, outs, f"rotation-l5i-20MHz-n_nc{n_nc}-prec{prec}")
+
+
+def test_ragged_batch_recordings_against_the_oracle():
+    # four recordings of the benchmark's 64-recording batch (seed 2024): L1 C/A 5 MHz x 8 steps,
+    # E1B 12 MHz, L5I 25 MHz with 1 and with 10 coherent periods (secondary-code search), each on
+    # planted and absent PRNs, run as one batch and compared with the oracle (the secondary-code
+    # recording on its first two accumulation steps and two PRNs, to bound the oracle's time)
+    from acqgb300 import batch as B
+    recs = synth.ragged_batch(seed=2024)
+    chosen = [recs[i] for i in (9, 13, 5, 11)]
+    for r in chosen:
+        planted = [s.prn for s in r["sats"]]
+        absent = [p for p in r["prns"] if p not in planted]
+        keep = 1 if r["n_coh"] > 1 else 2
+        r["prns"] = sorted(planted[:keep] + absent[:1])
+        if r["n_coh"] > 1:
+            r["n_nc"] = 2
+    cache = B.PlanCache()
+    items = B.batch_from_recordings(chosen, cache)
+    bt = B.AcquisitionBatch(items)
+    got = bt.run()
+    bt.close()
+    ties = 0
+    for r, res in zip(chosen, got):
+        name = r["system"].name
+        kw = dict(min_doppler_coverage=r["cov"], num_coherently_integrated_code_periods=r["n_coh"],
+                  num_noncoherent_accumulations=r["n_nc"])
+        outs = _oracles(name, r["fs"], r["prns"], r["samples"], **kw)
+        for g, a, b in zip(res, outs["f32"][0], outs["f64"][0]):
+            if (a.peak_doppler_bin, a.peak_code_bin) != (b.peak_doppler_bin, b.peak_code_bin):
+                ties += 1
+                continue
+            label = (name, r["n_coh"], g.prn)
+            assert (g.peak_doppler_bin, g.peak_code_bin) == (b.peak_doppler_bin, b.peak_code_bin), label
+            assert A.is_detected(g) == O.is_detected(b), label
+            assert g.secondary_code_phase == b.secondary_code_phase, label
+            assert float(g.noise_power) == pytest.approx(b.noise_power, rel=SCALAR_RTOL), label
+            assert float(g.peak_to_noise_ratio) == pytest.approx(b.peak_to_noise_ratio, rel=SCALAR_RTOL), label
+            assert g.code_phase == pytest.approx(b.code_phase, rel=SCALAR_RTOL, abs=1e-6), label
+            assert g.carrier_doppler == pytest.approx(b.carrier_doppler, rel=SCALAR_RTOL, abs=1e-3), label
+    print(f"[batch] near-ties {ties}")
+    assert ties <= 1

@@ -5,7 +5,8 @@ running (a receiver's real-time processing thread, where cudaMalloc/cudaFree may
 the device and stall it, or a plugin whose host framework owns all device memory). Given the
 power surface that acq_acquire stored, it must report the same peak cell and, within the
 tolerance of the parity tests, the same noise power, on consecutive calls that share its
-static scratch. This file is collected last on purpose.
+static scratch; and the oracle's estimators (src/est_signal_noise_power.jl:109-243) run on that
+same surface must agree. This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -15,6 +16,8 @@ import pytest
 import acqgb300 as A
 from acqgb300 import _lib as L
 from acqgb300 import synth
+from oracle import acq_oracle as O
+from oracle import gnss_codes as G
 
 pytestmark = pytest.mark.gpu
 
@@ -33,21 +36,30 @@ def _noalloc(power_bins: np.ndarray, fs: float, fc: float, estimator: int) -> L.
     return L.NoiseStats.from_buffer_copy(out.cpu().numpy().tobytes())
 
 
+KW = dict(min_doppler_coverage=5000, num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=2)
+
+
 def _acquired(estimator):
     fs = 5e6
     sats = [synth.Satellite(3, 44.0, 2300.0, 411.7), synth.Satellite(9, 41.0, -1800.0, 77.2)]
-    plan = A.plan_acquire(A.GPSL1CA(), fs, [3, 9, 12], min_doppler_coverage=5000,
-                          num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=2,
-                          noise_estimator=estimator)
+    plan = A.plan_acquire(A.GPSL1CA(), fs, [3, 9, 12], noise_estimator=estimator, **KW)
     x = synth.synth(A.GPSL1CA(), fs, 2 * 10 * plan.samples_per_code, sats, seed=31).astype(np.complex64)
     return A.acquire_b(plan, x, [3, 9, 12], store_power_bins=True), fs
 
 
-def _check(stats: L.NoiseStats, r):
+def _check(stats: L.NoiseStats, r, fs, est):
     assert (stats.peak_doppler_bin, stats.peak_code_bin) == (r.peak_doppler_bin, r.peak_code_bin)
     assert stats.peak_power == float(r.peak_power)
     assert stats.noise_power == pytest.approx(float(r.noise_power), rel=RTOL)
     assert stats.signal_power == pytest.approx(float(r.peak_power) - float(r.noise_power), rel=RTOL)
+    # the oracle's peak (lowest column, then lowest row) and FP64 noise estimate on the same surface
+    oplan = O.plan_acquire(G.GPSL1CA, fs, [r.prn], precision="f64",
+                           noise_estimator="global_mean" if est == L.ACQ_NOISE_GLOBAL_MEAN else "opposite_row", **KW)
+    surf = O.PrnSurface(r.power_bins.astype(np.float64), np.zeros(r.power_bins.shape, np.int32), "materialised")
+    peak, row, col = O.find_peak(surf, oplan)
+    assert (stats.peak_doppler_bin, stats.peak_code_bin) == (row, col)
+    assert stats.peak_power == np.float32(peak)
+    assert stats.noise_power == pytest.approx(O.noise_power(surf, oplan, row, col), rel=RTOL)
 
 
 def test_noalloc_matches_acquire_on_consecutive_calls():
@@ -57,7 +69,7 @@ def test_noalloc_matches_acquire_on_consecutive_calls():
     # several calls in a row share (and re-clear) the static scratch
     for r, est in [(res_or[0], L.ACQ_NOISE_OPPOSITE_ROW), (res_gm[1], L.ACQ_NOISE_GLOBAL_MEAN),
                    (res_or[2], L.ACQ_NOISE_OPPOSITE_ROW), (res_gm[0], L.ACQ_NOISE_GLOBAL_MEAN)]:
-        _check(_noalloc(r.power_bins, fs, fc, est), r)
+        _check(_noalloc(r.power_bins, fs, fc, est), r, fs, est)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
