@@ -236,7 +236,7 @@ class AcquisitionPlan:
         """Names of the kernels the last acquisition launched, in order (acq_plan_last_kernels)."""
         buf = C.create_string_buffer(8192)
         _check(L.load().acq_plan_last_kernels(self._h, buf, len(buf)))
-        return [k for k in buf.value.decode().split(",") if k]
+        return [k for k in buf.value.decode().split(";") if k]
 
     def set_form(self, form: str) -> str:
         """'plain' (one kernel per stage, the default) or 'fused' (cluster kernel where supported).

@@ -482,6 +482,12 @@ __global__ void k_extract(const float* __restrict__ acc, const uint16_t* __restr
         col = static_cast<int>(order / P.ndop);
         row = static_cast<int>(order - static_cast<uint32_t>(col) * P.ndop);
     }
+    // a key outside the surface can only come from a stage that gave up (its error word is set and
+    // the host reports it): keep every index below in bounds
+    if (order / P.ndop >= static_cast<uint32_t>(P.spc_eff) || col < 0 || col >= P.spc_eff) {
+        col = 0;
+        row = 0;
+    }
     // noise power (FP64 sums)
     double part = 0.0;
     int lo = 0, hi = -1;

@@ -245,6 +245,9 @@ struct ColTmaParams {
     const int* drift;      // (n_nc, ndop) in [0, spc)
     float* acc;            // (n_req, ndop, spc_eff)
     int* err;
+    // k_col_tma_k1: polls of each tile wait before the block gives up (kWaitLimit; a test sets
+    // 0 to run the give-up path); the wait for copies still in flight keeps the full limit
+    uint32_t wait_polls;
 };
 
 // Persistent column stage for all accumulation steps of the simple path. Work item = (requested
@@ -448,14 +451,11 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
             __syncthreads();
         }
         if (threadIdx.x == 0 && k + 1 < K) issue(k + 1);
-        if (!mbar_wait_bounded(&mbar[b], (phases >> b) & 1u, p.err, 1)) {
-            // give the copies in flight a bounded chance to land, then leave
-            mbar_wait_bounded(&mbar[b ^ 1], (phases >> (b ^ 1)) & 1u, p.err, 1);
-            return;
-        }
-        phases ^= 1u << b;
+        const bool landed = mbar_wait_bounded(&mbar[b], (phases >> b) & 1u, p.err, 1, p.wait_polls);
+        const uint32_t parity_b = (phases >> b) & 1u;
+        if (landed) phases ^= 1u << b;
         const int c0 = cb * W;
-        const int wv = min(W, p.spc - c0);
+        const int wv = landed ? min(W, p.spc - c0) : 0;
         const float2* tl = buf0 + b * BS;
         const int* om = sht + m * N2;
         for (int t = threadIdx.x; t < wv; t += blockDim.x) {
@@ -473,7 +473,17 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
                 *cell = __fadd_rn(*cell, pw);
             });
         }
-        __syncthreads();
+        // one block-wide decision: if any thread's wait gave up, thread 0 (which issued every copy)
+        // waits with the full limit for the copies still in flight into this block's buffers, then
+        // the whole block leaves (the error word is already set)
+        if (__syncthreads_or(!landed)) {
+            if (threadIdx.x == 0) {
+                if (!landed) mbar_wait_bounded(&mbar[b], parity_b, p.err, 1);
+                if (k + 1 < K) mbar_wait_bounded(&mbar[b ^ 1], (phases >> (b ^ 1)) & 1u, p.err, 1);
+            }
+            __syncthreads();
+            return;
+        }
         if (m == p.n_nc - 1) {
             float* ap = p.acc + static_cast<int64_t>(pi) * ND * p.spc_eff;
             const int span = wv + 2 * H;

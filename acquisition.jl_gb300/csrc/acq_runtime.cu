@@ -359,6 +359,7 @@ struct acq_plan {
     ColTmaFn col_k1 = nullptr;
     CUtensorMap tmapK1{};
     int k1W = 128, k1Grid = 1, k1CtasPerSm = 0;
+    uint32_t k1WaitPolls = kWaitLimit;   // ACQ_OPT_COLUMN_WAIT_POLLS (test-only)
     size_t smem_col_k1 = 0;
     // coherent tile as a correlation GEMM on the tensor cores (TMA simple path, block size <= 256):
     // time-domain operand blocks per (step, row), their inverse scales, one CTA per SM
@@ -1093,6 +1094,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         cp.box_rows = P->tmaBoxRows; cp.n_boxes = P->tmaBoxes; cp.n_cblk = (g.spc + P->tmaW - 1) / P->tmaW;
         cp.n_items = n * cp.n_cblk; cp.rows_per_step = nprn * g.ndop; cp.n1 = g.n_coh;
         cp.twD = P->fftD.tw; cp.drift = P->drift.as<int>(); cp.acc = P->accb.as<float>(); cp.err = P->errflag.as<int>();
+        cp.wait_polls = P->k1WaitPolls;
         t_begin(P, ACQ_KERNEL_COLUMN);
         if (P->col_k1) {
             cp.W = P->k1W;
@@ -1750,7 +1752,7 @@ int acq_plan_last_kernels(const acq_plan* P, char* buf, size_t len) {
     return guarded([&] {
         if (!P) throw AcqError(ACQ_ERR_ARGUMENT, "null plan");
         std::string out;
-        for (size_t i = 0; i < P->klog.size(); ++i) out += (i ? "," : "") + P->klog[i];
+        for (size_t i = 0; i < P->klog.size(); ++i) out += (i ? ";" : "") + P->klog[i];
         if (buf && len) {
             const size_t m = std::min(len - 1, out.size());
             std::memcpy(buf, out.data(), m);
@@ -1888,6 +1890,7 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_TILE_ROWS: *value = P->tile_fs ? P->tileRows : 0; break;
             case ACQ_OPT_TRANSFORM_LENGTH: *value = P->g.fft_tile; break;
             case ACQ_OPT_TILE_MMA: *value = P->tmma ? 1 : 0; break;
+            case ACQ_OPT_COLUMN_WAIT_POLLS: *value = P->col_k1 ? P->k1WaitPolls : 0; break;
             case ACQ_OPT_COLUMN_WIDTH: *value = P->col_k1 ? P->k1W : P->col_tma ? P->tmaW : 0; break;
             case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_k1 ? P->k1CtasPerSm : P->col_tma ? P->tmaCtasPerSm : 0; break;
             default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
@@ -2048,6 +2051,14 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             setup_col_tma(P, P->n_plan_prns, P->tmaW, P->tmaCtasPerSm);
             setup_tile_mma(P);
             if (effective) *effective = P->tmma ? 1 : 0;
+            return;
+        }
+        if (option == ACQ_OPT_COLUMN_WAIT_POLLS) {
+            if (value < 0 || value > static_cast<int64_t>(kWaitLimit))
+                throw AcqError(ACQ_ERR_ARGUMENT, "poll limit must be in 0:" + std::to_string(kWaitLimit));
+            CK(cudaStreamSynchronize(P->stream));
+            P->k1WaitPolls = static_cast<uint32_t>(value);
+            if (effective) *effective = P->col_k1 ? P->k1WaitPolls : 0;
             return;
         }
         if (option == ACQ_OPT_MMA_SCALE_LOG2) {

@@ -66,8 +66,12 @@ FS, N_COH, N_NC, COV = CFG["fs"], CFG["n_coh"], CFG["n_nc"], CFG["cov"]
 WORKLOAD = CFG["workload"]
 
 
+CONFIG_NAME = "cfg2"
+
+
 def set_config(name):
-    global CFG, FS, N_COH, N_NC, COV, WORKLOAD
+    global CFG, FS, N_COH, N_NC, COV, WORKLOAD, CONFIG_NAME
+    CONFIG_NAME = name
     CFG = CONFIGS[name]
     FS, N_COH, N_NC, COV, WORKLOAD = CFG["fs"], CFG["n_coh"], CFG["n_nc"], CFG["cov"], CFG["workload"]
 
@@ -77,17 +81,29 @@ def system_of(cfg):
     return {"GPSL1CA": A.GPSL1CA, "GPSL5I": A.GPSL5I, "GalileoE1B": A.GalileoE1B}[cfg["system"]]()
 
 
-def make_input():
-    from acqgb300 import synth
-    sysm = system_of(CFG)
+def make_input(host_model: bool = False):
+    """The workload's seeded recording and its satellites. host_model=False: the product's host
+    signal generator (acqgb300.synth, codes from libacqgb300); True: the oracle's restatement of
+    the same model (oracle.signal_model), which gives the same bytes without loading the product
+    library (the CPU legs use it)."""
+    if host_model:
+        from oracle import gnss_codes as G
+        from oracle import signal_model as synth
+        sysm = G.SYSTEMS[CFG["system"]]
+        code_length, code_freq = sysm.code_length, sysm.code_freq
+        Sat = synth.Sat
+    else:
+        from acqgb300 import synth
+        sysm = system_of(CFG)
+        code_length, code_freq = sysm.code_length, sysm.code_frequency
+        Sat = synth.Satellite
     rng = np.random.default_rng(SEED)
     if "fixed" in CFG:
-        sats = [synth.Satellite(p, c, d, cp) for (p, c, d, cp) in CFG["fixed"]]
+        sats = [Sat(p, c, d, cp) for (p, c, d, cp) in CFG["fixed"]]
     else:
         present = sorted(rng.choice(np.arange(1, 33), size=CFG["n_sats"], replace=False).tolist())
-        sats = synth.random_sats(rng, present, CFG["cn0"], CFG["dmax"], sysm.code_length,
-                                 bit_period_s=CFG["bit_period"])
-    spc = int(math.ceil(sysm.code_length / sysm.code_frequency * FS))
+        sats = synth.random_sats(rng, present, CFG["cn0"], CFG["dmax"], code_length, bit_period_s=CFG["bit_period"])
+    spc = int(math.ceil(code_length / code_freq * FS))
     n = N_NC * N_COH * spc
     x = synth.synth(sysm, FS, n, sats, SEED)
     if CFG["quant"] == "ci16":
@@ -95,6 +111,20 @@ def make_input():
     if CFG["quant"] == "ci8":
         return synth.to_ci8_3bit(x), sats
     return x.astype(np.complex64), sats
+
+
+def input_digest(sig) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(sig).tobytes()).hexdigest()[:16]
+
+
+def workload_config(sig, n_nc: int, geometry: dict) -> dict:
+    """The `config` of both arms (identical for the same workload): what is searched, on what input."""
+    return {"workload": WORKLOAD if n_nc == N_NC else f"{WORKLOAD}_nnc{n_nc}", "prns": len(PRNS),
+            "samples": int(n_nc * N_COH * geometry["spc"]), "num_doppler_bins": int(geometry["ndop"]),
+            "samples_per_code": int(geometry["spc"]), "fft_size": int(geometry["fft"]),
+            "input": f"seed {SEED}, {CFG['quant'] or 'cf32'}, sha256 {input_digest(sig)}",
+            "l2": "GPU arm: flushed (256 MB write) before every timed step; CPU arm: not applicable"}
 
 
 def as_complex64(sig):
@@ -182,27 +212,104 @@ class ClockSampler:
                 "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
 
 
-def cpu_port_sample():
-    """(accumulation steps timed per sample, scale factor to one 32-PRN acquisition)."""
-    n_nc = min(N_NC, 1 if CFG["system"] == "GPSL5I" and N_COH > 1 else N_NC)
-    return n_nc, len(PRNS) * N_NC / n_nc
+# ---- CPU baseline: the oracle's FP32 restatement with PRNs spread over a process pool, one
+# worker per host core, single-threaded FFTs in each (the reference's per-core PRN loop,
+# src/acquire.jl:142,195). Workers are spawned (never forked) and build their plan and input
+# once, outside every timed region.
+_POOL_STATE = None
 
 
-def cpu_port_time_per_prn(sig, steps: int = 1):
-    """Time the oracle's FP32 restatement for one PRN (all steps, or one step of a rotation search)."""
+def _pool_init(cfg_name, prns, n_nc):
+    global _POOL_STATE
+    set_config(cfg_name)
     from oracle import acq_oracle as O
     from oracle import gnss_codes as G
-    n_nc, _ = cpu_port_sample()
-    sig = as_complex64(sig)
-    plan = O.plan_acquire(G.SYSTEMS[CFG["system"]], FS, [1], min_doppler_coverage=COV,
+    O.FFT_WORKERS = 1
+    sig, _ = make_input(host_model=True)
+    plan = O.plan_acquire(G.SYSTEMS[CFG["system"]], FS, prns, min_doppler_coverage=COV,
                           num_coherently_integrated_code_periods=N_COH, bit_edge_search_steps=CFG["n_be"],
                           num_noncoherent_accumulations=n_nc, precision="f32")
-    times = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        O.acquire_b(plan, sig, [1])
-        times.append(time.perf_counter() - t0)
-    return times
+    _POOL_STATE = (plan, as_complex64(sig))
+
+
+def _pool_task(prns):
+    from oracle import acq_oracle as O
+    plan, sig = _POOL_STATE
+    return [(r.prn, r.peak_doppler_bin, r.peak_code_bin, bool(O.is_detected(r))) for r in O.acquire_b(plan, sig, prns)]
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+class CpuPool:
+    """A pool of spawned oracle workers for the current workload (n_nc accumulation steps)."""
+
+    def __init__(self, cfg_name: str, prns, n_nc: int, workers: int | None = None):
+        import multiprocessing as mp
+        for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+            os.environ[v] = "1"
+        self.workers = workers or host_cores()
+        self.prns = list(prns)
+        self.pool = mp.get_context("spawn").Pool(self.workers, initializer=_pool_init,
+                                                 initargs=(cfg_name, self.prns, n_nc))
+        self.pool.map(_pool_task, [[]] * self.workers)          # every worker initialised
+
+    def acquire(self, prns=None):
+        """One acquisition over `prns` (default: all), PRNs dealt round-robin to the workers."""
+        prns = self.prns if prns is None else list(prns)
+        groups = [prns[i::self.workers] for i in range(self.workers)]
+        out = []
+        for g in self.pool.map(_pool_task, [g for g in groups if g]):
+            out += g
+        return sorted(out, key=lambda r: prns.index(r[0]))
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()
+
+
+def cpu_sample_shape():
+    """(PRNs per timed sample, accumulation steps per sample): whole 32-PRN acquisitions where one
+    fits in a few seconds of the host's cores, else a bounded sample of one PRN per worker over one
+    accumulation step (the secondary-code rotation workloads)."""
+    if CFG["system"] == "GPSL5I" and N_COH > 1:
+        return min(len(PRNS), host_cores()), 1
+    return len(PRNS), N_NC
+
+
+def cpu_baseline_run(steps: int, warmup: int, budget_s: float | None = None):
+    """Time `steps` samples (after `warmup`) on the pool; with budget_s, as many as fit in that
+    many seconds (at least one). Returns (seconds per 32-PRN acquisition, per-sample times,
+    sample description, workers)."""
+    n_prn, n_nc = cpu_sample_shape()
+    pool = CpuPool(CONFIG_NAME, PRNS[:n_prn], n_nc)
+    try:
+        for _ in range(warmup):
+            pool.acquire()
+        ts = []
+        t_start = time.perf_counter()
+        while True:
+            t0 = time.perf_counter()
+            pool.acquire()
+            ts.append(time.perf_counter() - t0)
+            if budget_s is None:
+                if len(ts) >= steps:
+                    break
+            elif time.perf_counter() - t_start >= budget_s or len(ts) >= steps:
+                break
+    finally:
+        pool.close()
+    scale = (len(PRNS) / n_prn) * (N_NC / n_nc)
+    whole = scale == 1.0
+    desc = (f"whole {len(PRNS)}-PRN acquisitions of the oracle's FP32 restatement, PRNs spread over {pool.workers} "
+            f"spawned single-threaded workers" if whole else
+            f"{n_prn} PRNs x {n_nc} of {N_NC} accumulation steps per sample over {pool.workers} spawned "
+            f"single-threaded workers, scaled x{scale:g} to a 32-PRN acquisition")
+    return statistics.mean(ts) * scale, ts, desc, pool.workers
 
 
 def run_reference_batch(args):
@@ -292,29 +399,33 @@ def run_reference(args):
         return run_reference_batch(args)
     if args.config == "cfg5":
         return run_reference_fine(args)
-    ci16, _ = make_input()
-    warm = []
-    for _ in range(args.warmup):
-        warm += cpu_port_time_per_prn(ci16, 1)
-    # each step times one bounded sample; the number of timed samples is capped so the whole run
-    # stays within about two minutes of host time whatever --steps is
-    per_sample = min(warm) if warm else cpu_port_time_per_prn(ci16, 1)[0]
-    n_timed = max(1, min(args.steps, int(120.0 / max(per_sample, 1e-3))))
-    times = cpu_port_time_per_prn(ci16, n_timed)
-    per_acq = statistics.mean(times) * cpu_port_sample()[1]
+    from oracle import acq_oracle as O
+    from oracle import gnss_codes as G
+    sig, _ = make_input(host_model=True)
+    geo = O.plan_geometry(G.SYSTEMS[CFG["system"]], FS, min_doppler_coverage=COV, n_coh=N_COH, n_be=CFG["n_be"],
+                          n_nc=N_NC)
+    per_acq, ts, desc, workers = cpu_baseline_run(args.steps, args.warmup)
     value = 1.0 / per_acq
-    cores = os.cpu_count()
+    # the same restatement on the reference's CPU-runnable geometry (4 MHz, 1 ms, +-7 kHz, 32
+    # PRNs), beside the reference's own published figures for that geometry
+    cfg_name = CONFIG_NAME
+    set_config("cfg1")
+    t1, ts1, _, _ = cpu_baseline_run(20, 2)
+    set_config(cfg_name)
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_acq * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "impl": "reference", "timed_samples": n_timed,
-            "config": {"workload": WORKLOAD, "prns": 32, "samples": int(len(ci16))},
-            "cpu_baseline": {"value": value, "unit": "acq/s", "cores": cores, "kind": "port",
-                             "sample": f"1 PRN x {cpu_port_sample()[0]} accumulation step(s) per step, extrapolated to "
-                                       "32 PRNs x all steps; the Julia reference is unavailable here, its algorithm "
-                                       "runs as the oracle's FP32 numpy/scipy restatement (scipy.fft workers=-1)"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ts) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": f"synthetic (seeded, {CFG['quant'] or 'cf32'})", "impl": "reference",
+            "config": workload_config(sig, N_NC, {"spc": geo["spc"], "ndop": geo["ndop"], "fft": geo["F"]}),
+            "cpu_baseline": {"value": value, "unit": "acq/s", "cores": workers, "kind": "port",
+                             "sample": desc + "; the Julia reference is unavailable on this machine, its algorithm "
+                                              "runs as the oracle's FP32 numpy/scipy restatement"},
             "e2e": {"value": value, "unit": "acq/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "msample_prn_per_s": value * 32 * len(ci16) / 1e6}
+            "msample_prn_per_s": value * len(PRNS) * N_NC * N_COH * geo["spc"] / 1e6,
+            "port_on_cpu_runnable_geometry": {
+                "workload": CONFIGS["cfg1"]["workload"], "value": 1.0 / t1, "unit": "acq/s", "cores": workers,
+                "published_reference": {"1 thread": 25.0, "4 threads": 77.0, "8 threads": 118.0,
+                                        "source": "CHANGELOG.md:234-237 (v2.0.0 code, CPU unstated)"}}}
     print(json.dumps(line))
 
 
@@ -872,23 +983,20 @@ def main():
             "kernel_ms_per_step": {k: v[0] / args.steps for k, v in ktimes.items()}}
 
     cpu = None
-    if not args.no_cpu_baseline:
-        ts = cpu_port_time_per_prn(ci16, 1)
-        n_s, scale = cpu_port_sample()
-        per_acq = ts[0] * scale
-        cpu = {"value": 1.0 / per_acq, "unit": "acq/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"oracle FP32 numpy/scipy restatement, 1 PRN x {n_s} accumulation step(s), scaled to 32 PRNs "
-                         "x all steps (scipy.fft workers=-1)"}
+    if not args.no_cpu_baseline and not args.prns and n_nc == N_NC:
+        # about 15 s of host time, after every GPU measurement
+        per_acq, ts, desc, workers = cpu_baseline_run(10 ** 6, 1, budget_s=15.0)
+        cpu = {"value": 1.0 / per_acq, "unit": "acq/s", "cores": workers, "kind": "port",
+               "sample": f"{desc}; {len(ts)} samples in {sum(ts):.1f} s"}
     samples = n_nc * N_COH * spc
     det = [r.prn for r in res if A.is_detected(r)]
     line = {"metric": "32-PRN acquisitions/s", "value": value, "unit": "acq/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, CI16)",
-            "config": {"workload": WORKLOAD if n_nc == N_NC else f"{WORKLOAD}_nnc{n_nc}", "prns": n_prn, "samples": samples, "num_doppler_bins": ndop,
-                       "samples_per_code": spc, "fft_size": F, "form": form, "rotation_precision": main_prec,
-                       "launch_shapes": (dict(tuned["settings"], tuned_ms=tuned["ms"], default_ms=tuned["start_ms"])
-                                         if tuned else "defaults"),
-                       "l2": "flushed (256 MB write) before every timed step"},
+            "config": workload_config(ci16, n_nc, {"spc": spc, "ndop": ndop, "fft": F}),
+            "gpu_settings": {"form": form, "rotation_precision": main_prec,
+                             "launch_shapes": (dict(tuned["settings"], tuned_ms=tuned["ms"],
+                                                    default_ms=tuned["start_ms"]) if tuned else "defaults")},
             "msample_prn_per_s": value * n_prn * samples / 1e6,
             "other_form": {"form": other_form, "value": plain_value, "unit": "acq/s",
                            "kernel_ms_per_step": ({k: v[0] / args.steps for k, v in plain_ktimes.items()}

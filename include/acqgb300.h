@@ -160,8 +160,8 @@ int acq_plan_stream(const acq_plan* plan, void** stream);
 int acq_plan_last_launch_count(const acq_plan* plan, int64_t* count);
 
 /* Names of this library's kernels launched by the last acquisition on the plan, in launch
- * order, comma-separated; size-specialised kernels carry their template sizes, e.g.
- * "k_tile_stubs,k_tile_mma,k_col_tma_k1<20>,k_extract". Written NUL-terminated to buf (truncated
+ * order, separated by ';'; size-specialised kernels carry their template sizes, e.g.
+ * "k_tile_stubs;k_tile_mma;k_col_sign_sb<32,25,8,2>;k_extract". Written NUL-terminated to buf (truncated
  * to len). A replayed CUDA graph reports the sequence it was captured from. Diagnostic, for
  * tests that pin which instantiation a geometry runs; no reference counterpart. */
 int acq_plan_last_kernels(const acq_plan* plan, char* buf, size_t len);
@@ -194,6 +194,11 @@ int acq_plan_last_kernels(const acq_plan* plan, char* buf, size_t len);
 #define ACQ_OPT_TILE_MMA 11          /* block_size <= 256: the coherent tile as a time-domain correlation GEMM
                                         on the tensor cores (FP16 codes x FP16 hi + lo samples, FP32
                                         accumulation) = 1 (default where available), FP32 FFTs = 0 */
+#define ACQ_OPT_COLUMN_WAIT_POLLS 12 /* test-only: polls of each tile wait in the Doppler-group column stage before
+                                        the block gives up (default 2^24; 0 gives up at once and runs the
+                                        give-up path: one block-wide decision, a full-limit wait for the copies
+                                        in flight, ACQ_ERR_TIMEOUT from acq_fetch_results); 0 where the plan
+                                        has no such stage */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
  * form is used only where the plan's sizes have a fused kernel (otherwise plain).

@@ -248,12 +248,16 @@ def plan_geometry(system: System, fs: float, min_doppler_coverage: float = 7000.
                 step=step, R=R, bit_period_codes=bit_period_codes)
 
 
+# threads per FFT call (-1: all cores); a process pool that spreads PRNs over cores sets 1
+FFT_WORKERS = -1
+
+
 def _fft(x, axis, prec):
-    return sfft.fft(x, axis=axis, workers=-1)
+    return sfft.fft(x, axis=axis, workers=FFT_WORKERS)
 
 
 def _bfft(x, axis, prec):
-    return sfft.ifft(x, axis=axis, norm="forward", workers=-1)
+    return sfft.ifft(x, axis=axis, norm="forward", workers=FFT_WORKERS)
 
 
 def plan_acquire(system: System, sampling_freq: float, prns, *, min_doppler_coverage: float = 7000.0,
