@@ -8,7 +8,9 @@ import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libacqgb300.so")
+# ACQ_CHECKED_LIBRARY=1 loads the bounds-checked build (device index checks, debug use) instead
+LIB_PATH = os.path.join(_HERE, "libacqgb300_checked.so" if os.environ.get("ACQ_CHECKED_LIBRARY", "0") not in ("", "0")
+                        else "libacqgb300.so")
 
 ACQ_OK = 0
 ACQ_ERR_ARGUMENT = 1

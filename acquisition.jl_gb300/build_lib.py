@@ -1,6 +1,6 @@
 """Build libacqgb300.so in-tree (sm_103a only).
 
-    python acquisition.jl_gb300/build_lib.py [--debug]
+    python acquisition.jl_gb300/build_lib.py [--debug] [--bounds-check]
 
 Compiles the host C++ (g++) and the CUDA runtime/kernels (nvcc) in parallel and links
 ``acquisition.jl_gb300/acqgb300/libacqgb300.so``. No cmake. Host code is compiled with
@@ -21,6 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(HERE, "acqgb300")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libacqgb300.so")
+CHECKED_LIB = os.path.join(OUT_DIR, "libacqgb300_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,17 +39,24 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
-def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = False) -> str:
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = False, bounds_check: bool = False) -> str:
+    """Build the library; bounds_check=True builds the checked variant (device index checks that
+    record the first out-of-buffer access instead of faulting) as libacqgb300_checked.so, in its
+    own object directory. Returns the compiler output."""
+    build_dir = BUILD_DIR + ("_checked" if bounds_check else "")
+    lib = CHECKED_LIB if bounds_check else LIB
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     opt = ["-O0", "-g"] if debug else ["-O3"]
-    host_obj = os.path.join(BUILD_DIR, "acq_host.o")
-    dev_obj = os.path.join(BUILD_DIR, "acq_runtime.o")
-    na_obj = os.path.join(BUILD_DIR, "acq_noalloc.o")
-    corr_obj = os.path.join(BUILD_DIR, "acq_corr.o")
-    synth_obj = os.path.join(BUILD_DIR, "acq_synth.o")
+    if bounds_check:
+        opt = opt + ["-DACQ_BOUNDS_CHECK"]
+    host_obj = os.path.join(build_dir, "acq_host.o")
+    dev_obj = os.path.join(build_dir, "acq_runtime.o")
+    na_obj = os.path.join(build_dir, "acq_noalloc.o")
+    corr_obj = os.path.join(build_dir, "acq_corr.o")
+    synth_obj = os.path.join(build_dir, "acq_synth.o")
     inst = ["acq_inst_tile", "acq_inst_col", "acq_inst_sign", "acq_inst_mma"]
-    inst_objs = [os.path.join(BUILD_DIR, f"{n}.o") for n in inst]
+    inst_objs = [os.path.join(build_dir, f"{n}.o") for n in inst]
     host_cmd = ["g++", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", *opt,
                 f"-I{INCLUDE}", "-c", os.path.join(CSRC, "acq_host.cpp"), "-o", host_obj]
     dev_cmd = [nvcc, "-std=c++17", *ARCH, "-lineinfo", *opt, "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -71,10 +79,10 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
     cmds = [host_cmd, dev_cmd, na_cmd, corr_cmd, synth_cmd, *inst_cmds]
     with ThreadPoolExecutor(len(cmds)) as ex:
         outs = list(ex.map(_run, cmds))
-    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, na_obj, corr_obj, synth_obj, *inst_objs, "-o", LIB + ".tmp", "-lcudart_static", "-lrt", "-ldl",
+    link_cmd = [nvcc, "-shared", *ARCH, host_obj, dev_obj, na_obj, corr_obj, synth_obj, *inst_objs, "-o", lib + ".tmp", "-lcudart_static", "-lrt", "-ldl",
                 "-lpthread"]
     outs.append(_run(link_cmd))
-    os.replace(LIB + ".tmp", LIB)
+    os.replace(lib + ".tmp", lib)
     log = "".join(outs)
     if verbose:
         print(log)
@@ -82,5 +90,6 @@ def build(verbose: bool = False, debug: bool = False, ptxas_verbose: bool = Fals
 
 
 if __name__ == "__main__":
-    print(build(verbose=False, debug="--debug" in sys.argv, ptxas_verbose="-v" in sys.argv))
-    print("built", LIB)
+    checked = "--bounds-check" in sys.argv
+    print(build(verbose=False, debug="--debug" in sys.argv, ptxas_verbose="-v" in sys.argv, bounds_check=checked))
+    print("built", CHECKED_LIB if checked else LIB)

@@ -69,6 +69,12 @@ RotFsFn pick_rot_fs(int ndop);
 
 }  // namespace acq
 
+// the checked build's bounds table, per translation unit (no-ops in the normal build)
+cudaError_t acq_bounds_set_table_runtime(void* table);
+cudaError_t acq_inst_tile_set_bounds_table(void* table);
+cudaError_t acq_inst_col_set_bounds_table(void* table);
+cudaError_t acq_inst_sign_set_bounds_table(void* table);
+cudaError_t acq_inst_mma_set_bounds_table(void* table);
 cudaError_t acq_inst_tile_upload_twiddles(const float2* host, size_t n);
 cudaError_t acq_inst_col_upload_twiddles(const float2* host, size_t n);
 cudaError_t acq_inst_sign_upload_twiddles(const float2* host, size_t n);

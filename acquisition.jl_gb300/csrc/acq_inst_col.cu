@@ -57,3 +57,5 @@ ColTmaFn pick_col_tma(int ndop) {
 cudaError_t acq_inst_col_upload_twiddles(const float2* host, size_t n) {
     return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
 }
+
+ACQ_BC_SET_TABLE_IMPL(acq_inst_col_set_bounds_table)

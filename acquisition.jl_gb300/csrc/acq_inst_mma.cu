@@ -40,3 +40,5 @@ RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec,
 cudaError_t acq_inst_mma_upload_twiddles(const float2* host, size_t n) {
     return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
 }
+
+ACQ_BC_SET_TABLE_IMPL(acq_inst_mma_set_bounds_table)

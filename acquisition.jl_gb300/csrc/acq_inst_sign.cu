@@ -60,3 +60,5 @@ SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {
 cudaError_t acq_inst_sign_upload_twiddles(const float2* host, size_t n) {
     return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
 }
+
+ACQ_BC_SET_TABLE_IMPL(acq_inst_sign_set_bounds_table)

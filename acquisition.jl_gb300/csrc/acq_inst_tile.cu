@@ -36,3 +36,5 @@ FusedFn pick_fused(int fft, int ndop) {
 cudaError_t acq_inst_tile_upload_twiddles(const float2* host, size_t n) {
     return cudaMemcpyToSymbol(acq::c_regtw, host, sizeof(float2) * n);
 }
+
+ACQ_BC_SET_TABLE_IMPL(acq_inst_tile_set_bounds_table)

@@ -4,6 +4,7 @@
 
 #include <cstdint>
 
+#include "acq_bounds.cuh"
 #include "acq_fft.cuh"
 #include "acq_kernels_fs.cuh"
 #include "acqgb300.h"
@@ -13,6 +14,12 @@ namespace acq {
 // ------------------------------------------------------------------ sample loading
 // ComplexF32(x) with no scaling, src/acquire.jl:94,101.
 __device__ __forceinline__ float2 load_sample(const void* p, int dtype, int64_t i) {
+#ifdef ACQ_BOUNDS_CHECK
+    {
+        const unsigned sz = dtype == ACQ_CF32 ? 8u : dtype == ACQ_CI16 ? 4u : dtype == ACQ_CI8 ? 2u : 16u;
+        if (!bc_ok(static_cast<const char*>(p) + i * sz, sz, 1)) return make_float2(0.f, 0.f);
+    }
+#endif
     switch (dtype) {
         case ACQ_CF32: return reinterpret_cast<const float2*>(p)[i];
         case ACQ_CI16: {

@@ -8,6 +8,7 @@
 #include <cuda.h>
 #include <cstdint>
 
+#include "acq_bounds.cuh"
 #include "acq_fft.cuh"
 
 namespace acq {
@@ -126,7 +127,9 @@ __global__ void __launch_bounds__(256) k_col_simple_fs(const float2* __restrict_
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
     for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - e * W;
-        sm[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 40) v = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        sm[w] = v;
     }
     for (int i = threadIdx.x; i < ND; i += blockDim.x) dr[i] = has_drift ? drift[i] : 0;
     __syncthreads();
@@ -443,7 +446,8 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
                 if (mm == p.n_nc) {
                     rowof[k2] = row;
                 } else {
-                    int sh = p.drift[mm * ND + row];
+                    int sh = 0;
+                    ACQ_BC(&p.drift[mm * ND + row], 30) sh = p.drift[mm * ND + row];
                     if (sh > p.spc / 2) sh -= p.spc;
                     sht[i] = k2 * AW + H + sh;
                 }
@@ -505,19 +509,19 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
                     if (c < 0) c += p.spc;
                     if (c >= p.spc) c -= p.spc;
                     if (H == 0 || (lc >= H && lc < wv - H)) {
-                        arow[c] = v;
+                        ACQ_BC(&arow[c], 31) arow[c] = v;
                         const uint32_t ord = static_cast<uint32_t>(c) * ND + row;
                         if (v > bv || (v == bv && ord < bo)) {
                             bv = v;
                             bo = ord;
                         }
                     } else if (v != 0.f) {
-                        atomicAdd(arow + c, v);
+                        ACQ_BC(arow + c, 32) atomicAdd(arow + c, v);
                     }
                 }
                 if (p.rowpart) {   // FP32 across the warp, FP64 across column blocks (in the extraction)
                     for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
-                    if (lane == 0) rowpart_item(p, pi, cb, ND)[row] = static_cast<double>(rs);
+                    if (lane == 0) ACQ_BC(&rowpart_item(p, pi, cb, ND)[row], 33) rowpart_item(p, pi, cb, ND)[row] = static_cast<double>(rs);
                 }
             }
             if (p.peakpart) {
@@ -533,7 +537,8 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
                 if (threadIdx.x == 0) {
                     unsigned long long b = kred[0];
                     for (int w = 1; w < static_cast<int>(blockDim.x / 32); ++w) b = kred[w] > b ? kred[w] : b;
-                    p.peakpart[static_cast<int64_t>(pi) * p.npk + k1 * p.n_cblk + cb] = b;
+                    ACQ_BC(&p.peakpart[static_cast<int64_t>(pi) * p.npk + k1 * p.n_cblk + cb], 34)
+                        p.peakpart[static_cast<int64_t>(pi) * p.npk + k1 * p.n_cblk + cb] = b;
                 }
                 __syncthreads();
                 if (threadIdx.x < blockDim.x / 32) kred[threadIdx.x] = 0ULL;   // the accumulator starts at zero
@@ -709,9 +714,14 @@ __device__ __forceinline__ void scatter_rmw_rt(const float* __restrict__ stg, co
             const int w = w0 + u * nthr;
             const int row = w / W, t = w - (w / W) * W;
             ok[u] = w < n && t < wv;
-            int dc = c0 + t + (ok[u] ? drift[row] : 0);
+            int dr = 0;
+            if (ok[u]) ACQ_BC(&drift[row], 42) dr = drift[row];
+            int dc = c0 + t + dr;
             dc = dc >= spc ? dc - spc : dc;
             idx[u] = static_cast<int64_t>(row) * spc_eff + col0 + dc;
+#ifdef ACQ_BOUNDS_CHECK
+            if (ok[u]) ok[u] = bc_ok(&ap[idx[u]], 4u, 43) && (!(first & 2) || bc_ok(&wp[idx[u]], 2u, 44));
+#endif
         }
         if (!(first & 1)) {
 #pragma unroll
@@ -779,7 +789,9 @@ __global__ void __launch_bounds__(256) k_col_sign_fs(const float2* __restrict__ 
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
     for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - e * W;
-        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 41) v = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        tile[w] = v;
         stage[w] = 0.f;
         wst[w] = 0;
     }
@@ -842,7 +854,9 @@ __global__ void __launch_bounds__(256) k_col_rot_fs(const float2* __restrict__ T
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
     for (int w = threadIdx.x; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - e * W;
-        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 41) v = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        tile[w] = v;
     }
     for (int t = threadIdx.x; t < W; t += blockDim.x) {
         const int pc = c0 + t;
@@ -931,7 +945,9 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
     for (int w = tid; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - e * W;
-        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 41) v = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        tile[w] = v;
     }
     for (int i = tid; i < ND; i += blockDim.x) tws[i] = twD[i];
     if (tid < W) {
@@ -1048,7 +1064,9 @@ __global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W)
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
     for (int w = tid; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - (w / W) * W;
-        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * spc + c0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 41) v = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        tile[w] = v;
     }
     for (int i = tid; i < ND; i += blockDim.x) tws[i] = twD[i];
     if (tid < NP * NDB) {

@@ -182,7 +182,9 @@ __global__ void __launch_bounds__(256, 2) k_rot_mma(RotMmaParams p) {
     const float2* tp = p.T + static_cast<int64_t>(pi) * ND * p.spc;
     for (int w = tid; w < ND * W; w += blockDim.x) {
         const int e = w / W, t = w - (w / W) * W;
-        tile[w] = t < wv ? tp[static_cast<int64_t>(e) * p.spc + c0 + t] : make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f);
+        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * p.spc + c0 + t], 50) v = tp[static_cast<int64_t>(e) * p.spc + c0 + t];
+        tile[w] = v;
     }
     for (int i = tid; i < ND; i += blockDim.x) tws[i] = p.twD[i];
     if (tid < W) {

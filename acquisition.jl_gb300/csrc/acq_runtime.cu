@@ -7,9 +7,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -23,6 +25,8 @@
 #include "acq_tile_mma.cuh"
 
 using namespace acq;
+
+ACQ_BC_SET_TABLE_IMPL(acq_bounds_set_table_runtime)
 
 namespace {
 std::mutex g_name_mu;
@@ -144,7 +148,9 @@ __global__ void k_edge_peaks(const float* __restrict__ acc, int ndop, int spc, i
         int c = b + o;
         if (c < 0) c += spc;
         if (c >= spc) c -= spc;
-        const unsigned long long key = peak_key(ap[static_cast<int64_t>(r) * spc_eff + c], static_cast<uint32_t>(c) * ndop + r);
+        float v = 0.f;
+        ACQ_BC(&ap[static_cast<int64_t>(r) * spc_eff + c], 20) v = ap[static_cast<int64_t>(r) * spc_eff + c];
+        const unsigned long long key = peak_key(v, static_cast<uint32_t>(c) * ndop + r);
         best = key > best ? key : best;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -156,7 +162,7 @@ __global__ void k_edge_peaks(const float* __restrict__ acc, int ndop, int spc, i
     if (threadIdx.x == 0) {
         unsigned long long m = kred[0];
         for (int w = 1; w < static_cast<int>(blockDim.x / 32); ++w) m = kred[w] > m ? kred[w] : m;
-        peakpart[static_cast<int64_t>(pi) * npk + slot0 + j] = m;
+        ACQ_BC(&peakpart[static_cast<int64_t>(pi) * npk + slot0 + j], 21) peakpart[static_cast<int64_t>(pi) * npk + slot0 + j] = m;
     }
 }
 
@@ -176,14 +182,93 @@ __global__ void k_zero_edges(float* __restrict__ acc, int64_t rows, int spc, int
         int c = b + o;
         if (c < 0) c += spc;
         if (c >= spc) c -= spc;
-        acc[r * spc_eff + c] = 0.f;
+        ACQ_BC(&acc[r * spc_eff + c], 22) acc[r * spc_eff + c] = 0.f;
     }
 }
+
+#ifdef ACQ_BOUNDS_CHECK
+// Checked build: every device allocation of the library (and the caller's input of the current
+// request) is registered in a per-device table that the instrumented kernels check against.
+namespace bc {
+std::mutex mu;
+struct DeviceTable {
+    BoundsTable* d = nullptr;
+    std::map<unsigned long long, unsigned long long> ranges;   // base -> end
+};
+std::map<int, DeviceTable>& tables() {
+    static std::map<int, DeviceTable> t;
+    return t;
+}
+// (lock held) the current device's table, created and handed to every translation unit on first use
+DeviceTable& current() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    DeviceTable& t = tables()[dev];
+    if (!t.d) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, sizeof(BoundsTable)) != cudaSuccess) throw AcqError(ACQ_ERR_ALLOC, "bounds table");
+        cudaMemset(p, 0, sizeof(BoundsTable));
+        t.d = static_cast<BoundsTable*>(p);
+        for (auto set : {acq_bounds_set_table_runtime, acq_inst_tile_set_bounds_table, acq_inst_col_set_bounds_table,
+                         acq_inst_sign_set_bounds_table, acq_inst_mma_set_bounds_table})
+            if (set(p) != cudaSuccess) throw AcqError(ACQ_ERR_CUDA, "bounds table upload");
+    }
+    return t;
+}
+void upload(DeviceTable& t) {
+    if (t.ranges.size() > static_cast<size_t>(kBcMaxRanges)) throw AcqError(ACQ_ERR_UNSUPPORTED, "bounds table full");
+    std::vector<unsigned long long> b(kBcMaxRanges, 0), e(kBcMaxRanges, 0);
+    int n = 0;
+    for (auto& kv : t.ranges) {
+        b[n] = kv.first;
+        e[n] = kv.second;
+        ++n;
+    }
+    cudaDeviceSynchronize();
+    cudaMemcpy(t.d->base, b.data(), sizeof(unsigned long long) * kBcMaxRanges, cudaMemcpyHostToDevice);
+    cudaMemcpy(t.d->end, e.data(), sizeof(unsigned long long) * kBcMaxRanges, cudaMemcpyHostToDevice);
+    cudaMemcpy(&t.d->n, &n, sizeof(int), cudaMemcpyHostToDevice);
+}
+void add(const void* p, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu);
+    DeviceTable& t = current();
+    const unsigned long long a = reinterpret_cast<unsigned long long>(p);
+    t.ranges[a] = a + bytes;
+    upload(t);
+}
+void remove(const void* p) {
+    std::lock_guard<std::mutex> lk(mu);
+    DeviceTable& t = current();
+    t.ranges.erase(reinterpret_cast<unsigned long long>(p));
+    upload(t);
+}
+// after the stream has finished: report (and clear) the first skipped access
+void check() {
+    std::lock_guard<std::mutex> lk(mu);
+    DeviceTable& t = current();
+    constexpr size_t kTail = sizeof(BoundsTable) - offsetof(BoundsTable, err_site);   // err_site .. hits
+    static BoundsTable h;
+    cudaMemcpy(&h.err_site, &t.d->err_site, kTail, cudaMemcpyDeviceToHost);
+    if (h.err_site != 0) {
+        const int site = h.err_site;
+        const unsigned long long addr = h.err_addr, hits = h.hits;
+        cudaMemset(&t.d->err_site, 0, kTail);
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "device bounds check: access at 0x%llx (site %d) outside every buffer; %llu accesses skipped",
+                      addr, site, hits);
+        throw AcqError(ACQ_ERR_CUDA, buf);
+    }
+}
+}  // namespace bc
+#endif
 
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
     void reset() {
+#ifdef ACQ_BOUNDS_CHECK
+        if (p) bc::remove(p);
+#endif
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
@@ -198,6 +283,9 @@ struct DevBuf {
             throw AcqError(ACQ_ERR_ALLOC, "cudaMalloc(" + std::to_string(n) + ") failed: " + cudaGetErrorString(e));
         }
         bytes = n;
+#ifdef ACQ_BOUNDS_CHECK
+        bc::add(p, n);
+#endif
     }
     template <class T>
     T* as() const { return static_cast<T*>(p); }
@@ -1305,6 +1393,9 @@ void enqueue_acquire(acq_plan* P, const void* d_in, int dtype, int64_t n_samples
     LaunchArgs a;
     prepare_request(P, n_samples, prns, n, interm_freq, slots, offs, a.use_if, a.if_step);
     CK(cudaSetDevice(P->device));
+#ifdef ACQ_BOUNDS_CHECK
+    if (d_in != P->input.p) bc::add(d_in, static_cast<size_t>(n_samples) * sample_bytes(dtype));   // caller's buffer
+#endif
     cudaStream_t st = P->stream;
     // [slots (n) | PRN ids (n) | IF offsets (n_nc)] in one copy from page-locked memory
     const size_t bytes = sizeof(int) * 2 * static_cast<size_t>(n) + sizeof(float) * offs.size();
@@ -1534,6 +1625,9 @@ void fetch(acq_plan* P, acq_result* results, float* power_bins) {
     }
     CK(cudaStreamSynchronize(P->stream));
     t_collect(P);
+#ifdef ACQ_BOUNDS_CHECK
+    bc::check();
+#endif
     if (res_bytes) std::memcpy(results, hres, res_bytes);
     if (P->errflag.p) {
         const int e = *herr;
@@ -2164,6 +2258,10 @@ int acq_last_error(char* buf, size_t len) {
     return ACQ_OK;
 }
 
+#ifdef ACQ_BOUNDS_CHECK
+const char* acq_version(void) { return "acqgb300 0.1.0 sm_103a bounds-checked"; }
+#else
 const char* acq_version(void) { return "acqgb300 0.1.0 sm_103a"; }
+#endif
 
 }  // extern "C"

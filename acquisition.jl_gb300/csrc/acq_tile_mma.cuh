@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __r
     if (mx > 0.f) frexpf(mx, &ex);
     ex = max(-100, min(100, ex));
     const float s = ldexpf(1.f, 15 - ex);
-    if (tid == 0) inv_scale[static_cast<int64_t>(step) * G + rho] = ldexpf(1.f, ex - 15);
+    if (tid == 0) ACQ_BC(&inv_scale[static_cast<int64_t>(step) * G + rho], 3)
+        inv_scale[static_cast<int64_t>(step) * G + rho] = ldexpf(1.f, ex - 15);
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
         const int t = tid + i * kTmmaStubThreads;
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __r
         w.y = static_cast<uint32_t>(src[2]) | (static_cast<uint32_t>(src[3]) << 16);
         w.z = static_cast<uint32_t>(src[4]) | (static_cast<uint32_t>(src[5]) << 16);
         w.w = static_cast<uint32_t>(src[6]) | (static_cast<uint32_t>(src[7]) << 16);
-        out[idx] = w;
+        ACQ_BC(&out[idx], 2) out[idx] = w;
     }
 }
 
@@ -243,7 +244,8 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const int b = kc * 8 + e;
-                const uint32_t h = b < p.bs ? __half_as_ushort(__int2half_rn(c[b])) : 0u;
+                uint32_t h = 0u;
+                if (b < p.bs) ACQ_BC(&c[b], 5) h = __half_as_ushort(__int2half_rn(c[b]));
                 w[e >> 1] |= h << ((e & 1) * 16);
             }
         }
@@ -269,6 +271,12 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
             auto prefetch = [&](int u) {
                 const int b = u & 1;
                 ++n_s[b];
+#ifdef ACQ_BOUNDS_CHECK
+                if (!bc_ok(p.stubs + static_cast<int64_t>(u0 + u) * row_bytes, row_bytes, 4)) {
+                    mbar_expect_tx(&sbar[b], 0u);   // completes the phase without a copy
+                    return;
+                }
+#endif
                 mbar_expect_tx(&sbar[b], row_bytes);
                 bulk_load(stub0 + b * row_bytes, p.stubs + static_cast<int64_t>(u0 + u) * row_bytes, row_bytes,
                           &sbar[b]);
@@ -366,7 +374,8 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
 #pragma unroll
                     for (int e = 0; e < 16; ++e) {
                         const int64_t off = __shfl_sync(0xffffffffu, ol, (i & 31) + e);
-                        if (off >= 0 && jok) __stcs(base + off, make_float2(re[cb][e] * isc, im[cb][e] * isc));
+                        if (off >= 0 && jok)
+                            ACQ_BC(base + off, 6) __stcs(base + off, make_float2(re[cb][e] * isc, im[cb][e] * isc));
                     }
                     tc_wait_ld();
                 }

@@ -372,7 +372,7 @@ def _half_swap_rows(ndop: int) -> np.ndarray:
     return np.where(w < half, w + half, w - half)
 
 
-def sign_search_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray):
+def sign_search_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray, record: dict | None = None):
     """Data-bit / bit-edge search for each column of ``cim``.
 
     src/noncoherent_integration.jl:60-115 (``_sign_search_column!``) driven by
@@ -405,6 +405,8 @@ def sign_search_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray
             for b in range(ndb):
                 comb = (comb + plan.rdt(pats[b * coh_per_bit, p]) * subs[b]).astype(plan.cdt)
             pw = abs2(comb).astype(plan.rdt)
+            if record is not None:   # raw-bin power of candidate (e, p), keyed by its winner code
+                record[e * num_pat + p] = pw
             # first half-loop (w < half) then second half-loop; strict > per cell
             for sel in (slice(0, half), slice(half, ndop)):
                 w = np.arange(ndop)[sel]
@@ -416,7 +418,8 @@ def sign_search_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray
     return stage, winner
 
 
-def rotation_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray, chunk: int = 2048):
+def rotation_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray, chunk: int = 2048,
+                   record: dict | None = None):
     """Secondary-code rotation search for each column.
 
     src/noncoherent_integration.jl:183-297 (``_rotation_column!``) driven by :654-686.
@@ -453,6 +456,9 @@ def rotation_stage(cim: np.ndarray, plan: Plan, prn: int, cp_cols: np.ndarray, c
             # combine[q, w, c] = sum_p tiled[w, p, q] * subs[p, w, c]
             comb = np.einsum("wpq,pwc->qwc", tiled, subs, optimize=True).astype(plan.cdt)
             pw = abs2(comb).astype(plan.rdt)
+            if record is not None:   # (rotation slice, winner code) -> raw-bin power (one chunk)
+                for q in range(Q):
+                    record[(q // combos, e * combos + q % combos)] = pw[q]
             for q in range(Q):
                 ri = q // combos
                 if not use_max:
@@ -565,6 +571,28 @@ def noise_power(surf: PrnSurface, plan: Plan, peak_row: int, peak_col: int) -> f
 # --------------------------------------------------------------------------------------
 # secondary-code phase, src/acquire.jl:503-538
 # --------------------------------------------------------------------------------------
+def candidate_powers(plan: Plan, signal, prn: int, row: int, col: int, interm_freq_hz: float = 0.0) -> dict:
+    """Power of every data-bit / bit-edge candidate at surface cell (row, col) in the last
+    accumulation step, keyed by the winner code the surface records there (edge * patterns +
+    pattern; edge * combinations + combination within the rotation slice of `col`). The stage
+    keeps the first strict maximum of these (src/noncoherent_integration.jl:99-112,278-293);
+    candidates tied in exact arithmetic are broken by rounding. Test helper for the sign and
+    rotation paths."""
+    segs = all_segment_ffts(plan, signal, interm_freq_hz)
+    m = len(segs) - 1
+    cim = coherent_matrix(segs[m], plan.prn_conj_ffts[prn], plan)
+    spc = plan.samples_per_code
+    s_slice, c = divmod(col, spc)
+    src = (c - int(code_drift_shifts(plan, m)[row])) % spc
+    raw = np.where(_half_swap_rows(plan.num_doppler_bins) == row)[0]
+    rec: dict = {}
+    if plan.rotation_active:
+        rotation_stage(cim[:, [src]], plan, prn, np.array([src]), record=rec)
+        return {k[1]: float(max(v[w, 0] for w in raw)) for k, v in rec.items() if k[0] == s_slice}
+    sign_search_stage(cim[:, [src]], plan, prn, np.array([src]), record=rec)
+    return {k: float(max(v[w, 0] for w in raw)) for k, v in rec.items()}
+
+
 def estimate_secondary_code_phase(plan: Plan, prn: int, signal, interm_freq_hz: float,
                                   code_phase: float, doppler_hz: float) -> int:
     system = plan.system
