@@ -1,4 +1,6 @@
 // acq_inst_sign.cu — data-bit / bit-edge and secondary-code rotation stages for hot ndop.
+#include <cstdlib>
+
 #include "acq_inst.h"
 
 namespace acq {
@@ -41,7 +43,7 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
 }
 
 #define ACQ_SSB_CASE(N1, N2, W, NDB)                                                                 \
-    if (ndop == N1 * N2 && ndb == NDB) {                                                              \
+    if (ndop == N1 * N2 && ndb == NDB && (want_w == 0 || want_w == W)) {                              \
         *w = W;                                                                                      \
         *threads = (1 << (NDB - 1)) * N1 * W;                                                         \
         *smem = sizeof(float2) * ((size_t)(1 + NDB) * N1 * N2 * W + N1 * N2) + 64;                    \
@@ -50,7 +52,11 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
     }
 
 SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {
-    ACQ_SSB_CASE(32, 25, 8, 2) ACQ_SSB_CASE(32, 20, 8, 2) ACQ_SSB_CASE(32, 40, 4, 2) ACQ_SSB_CASE(20, 20, 8, 2)
+    // columns per block: the first instantiation listed for the size (ndop 800: four columns, two
+    // CTAs per SM, 5.81 ms vs 6.29 ms with eight on the 40 ms x 2 search), or ACQ_SIGN_W when set
+    const char* e = std::getenv("ACQ_SIGN_W");
+    const int want_w = e ? std::atoi(e) : 0;
+    ACQ_SSB_CASE(32, 25, 4, 2) ACQ_SSB_CASE(32, 25, 8, 2) ACQ_SSB_CASE(32, 20, 8, 2) ACQ_SSB_CASE(32, 40, 4, 2) ACQ_SSB_CASE(20, 20, 8, 2)
     ACQ_SSB_CASE(16, 25, 8, 1) ACQ_SSB_CASE(20, 10, 16, 2)
     return nullptr;
 }

@@ -1045,7 +1045,7 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
 // patterns' maxima are merged at the end in candidate order (e, p) (strict '>', earlier wins).
 // Same result as k_col_sign_fs. Block: NP * N1 * W threads.
 template <int N1, int N2, int W, int NDB>
-__global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W)
+__global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W, ((1 << (NDB - 1)) * N1 * W <= 256) ? 2 : 1)
     k_col_sign_sb(const float2* __restrict__ T, int spc, const float2* __restrict__ twD, const float* __restrict__ pats,
                   int n_coh, int n_be, int edge_step, const int* __restrict__ slots, const int* __restrict__ drift,
                   int first, float* __restrict__ acc, uint16_t* __restrict__ win, int spc_eff) {
