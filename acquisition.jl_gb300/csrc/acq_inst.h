@@ -48,12 +48,6 @@ SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem);
 
 struct RotMmaParams;
 struct DftMmaParams;
-struct RotTcParams;
-using RotTcFn = void (*)(RotTcParams);
-// rotation search with its first pass as a tensor-core GEMM (FP16 hi + lo) for (coherent periods,
-// blocks per period, data-bit combinations) and R rotations; nullptr when not instantiated.
-// *smem = dynamic bytes, *mt = M tiles of the A operand, *kch = its 16-byte K chunks per row.
-RotTcFn pick_rot_tc(int n_coh, int nb, int combos, int R, size_t* smem, int* mt, int* kch);
 using DftMmaFn = void (*)(DftMmaParams);
 using RotMmaFn = void (*)(RotMmaParams);
 // tensor-core rotation combine for (coherent periods, blocks per period, candidates) at an

@@ -2,7 +2,6 @@
 #include "acqgb300.h"
 #include "acq_inst.h"
 #include "acq_mma.cuh"
-#include "acq_rot_tc.cuh"
 
 namespace acq {
 
@@ -33,21 +32,6 @@ RotMmaFn pick_rot_mma(int n_coh, int nb, int n_candidates, int combos, int prec,
     const int qp = (n_candidates + 7) / 8 * 8;
     ACQ_MMA_CASE(20, 25, 24, 2) ACQ_MMA_CASE(10, 20, 16, 1) ACQ_MMA_CASE(20, 12, 24, 2) ACQ_MMA_CASE(10, 16, 16, 1)
     ACQ_MMA_CASE(10, 4, 16, 1) ACQ_MMA_CASE(20, 20, 24, 2)
-    return nullptr;
-}
-
-#define ACQ_RTC_CASE(NC, NB, CB)                                                                 \
-    if (n_coh == NC && nb == NB && combos == CB) {                                               \
-        using S = RotTcShape<NC, NB, CB>;                                                         \
-        *smem = S::smem_bytes(R);                                                                 \
-        *mt = S::mt(R);                                                                           \
-        *kch = S::KCH;                                                                            \
-        return named(&k_rot_tc<NC, NB, CB>, "k_rot_tc<" #NC "," #NB "," #CB ">");                 \
-    }
-
-RotTcFn pick_rot_tc(int n_coh, int nb, int combos, int R, size_t* smem, int* mt, int* kch) {
-    ACQ_RTC_CASE(20, 25, 2) ACQ_RTC_CASE(10, 20, 1) ACQ_RTC_CASE(20, 12, 2) ACQ_RTC_CASE(10, 16, 1)
-    ACQ_RTC_CASE(10, 4, 1) ACQ_RTC_CASE(20, 20, 2)
     return nullptr;
 }
 

@@ -21,7 +21,6 @@
 #include "acq_host.h"
 #include "acq_inst.h"
 #include "acq_mma.cuh"
-#include "acq_rot_tc.cuh"
 #include "acq_kernels.cuh"
 #include "acq_tile_mma.cuh"
 
@@ -428,11 +427,6 @@ struct acq_plan {
     // tensor-core rotation combine (ACQ_OPT_ROTATION_PRECISION != FP32)
     RotMmaFn rot_mma = nullptr;
     size_t smem_mma = 0;
-    // FP16 split precision: the first pass as a tensor-core GEMM (one A operand per PRN slot)
-    RotTcFn rot_tc = nullptr;
-    size_t smem_rtc = 0;
-    DevBuf rotA;
-    int rtcABytes = 0;
     int rot_prec = ACQ_PREC_FP32;
     // tensor-core Doppler DFT of the simple path (ACQ_OPT_DOPPLER_PRECISION != FP32)
     DftMmaFn dft_mma = nullptr;
@@ -715,56 +709,6 @@ void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
 // (bs <= 256) and ACQ_OPT_TILE_MMA is on, for all steps in one launch on the TMA simple path and
 // one launch per step on the others. The FP32 FFT tiles stay the fallback (and ACQ_GENERIC_FFT
 // keeps the generic kernels).
-// The rotation search's first pass on the tensor cores (FP16 hi + lo): picks the kernel for the
-// plan's sizes and builds, per PRN slot, the A operand M[rho, (p, re|im)] = W_NC^(p k1) s_q[p] with
-// rho = (r NC + k1) CB + d and q = r CB + d (the pattern order of the FP32 kernels), split into
-// FP16 hi + lo in the K-major no-swizzle layout of 8-row x 16-byte core matrices. nullptr when the
-// plan's sizes have no instantiation.
-RotTcFn setup_rot_tc(acq_plan* P) {
-    const Geometry& g = P->g;
-    const int CB = 1 << (g.ndb - 1);
-    size_t smem = 0;
-    int mt = 0, kch = 0;
-    RotTcFn fn = pick_rot_tc(g.n_coh, g.nb, CB, g.R, &smem, &mt, &kch);
-    if (!fn || smem > static_cast<size_t>(kSmemOptIn)) return nullptr;
-    const int NC = g.n_coh, tile_bytes = 16 * kch * 128;
-    const int a_bytes = 2 * mt * tile_bytes;
-    const int n_slots = static_cast<int>(P->prns.size());
-    std::vector<uint8_t> h(static_cast<size_t>(a_bytes) * n_slots, 0);
-    for (int sl = 0; sl < n_slots; ++sl) {
-        const std::vector<float> pat = sign_patterns(P->desc.system, P->prns[sl], g.ndb, g.R, g.n_coh,
-                                                     g.use_secondary_code != 0);   // [q][p]
-        uint8_t* base = h.data() + static_cast<size_t>(sl) * a_bytes;
-        for (int r = 0; r < g.R; ++r)
-            for (int k1 = 0; k1 < NC; ++k1)
-                for (int d = 0; d < CB; ++d) {
-                    const int rho = (r * NC + k1) * CB + d, q = r * CB + d;
-                    for (int pp = 0; pp < NC; ++pp) {
-                        const double a = -2.0 * M_PI * static_cast<double>((pp * k1) % NC) / NC;
-                        const double s = pat[static_cast<size_t>(q) * NC + pp];
-                        const double v[2] = {s * std::cos(a), s * std::sin(a)};
-                        for (int part = 0; part < 2; ++part) {
-                            const int k = 2 * pp + part, row = rho & 127;
-                            const size_t off = static_cast<size_t>(rho >> 7) * tile_bytes + (row >> 3) * (kch * 128) +
-                                               (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
-                            const __half hi = __float2half_rn(static_cast<float>(v[part]));
-                            const __half lo = __float2half_rn(static_cast<float>(v[part] - static_cast<double>(__half2float(hi))));
-                            std::memcpy(base + off, &hi, 2);
-                            std::memcpy(base + static_cast<size_t>(mt) * tile_bytes + off, &lo, 2);
-                        }
-                    }
-                }
-    }
-    P->rotA.ensure(h.size());
-    CK(cudaMemcpy(P->rotA.p, h.data(), h.size(), cudaMemcpyHostToDevice));
-    set_smem((const void*)fn, smem);
-    P->errflag.ensure(sizeof(int));
-    CK(cudaMemset(P->errflag.p, 0, sizeof(int)));
-    P->smem_rtc = smem;
-    P->rtcABytes = a_bytes;
-    return fn;
-}
-
 bool tile_mma_possible(const acq_plan* P) {
     return P->tmma_enabled && P->g.bs <= kTmmaMaxBs && !getenv_flag("ACQ_NO_TILE_MMA") &&
            !getenv_flag("ACQ_GENERIC_FFT");
@@ -1336,22 +1280,6 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             klog(P, nullptr, "k_col_simple");
             k_col_simple<<<dim3((g.spc + W - 1) / W, n), kThreads, P->smem_simple, st>>>(
                 P->T.as<float2>(), g.ndop, g.spc, W, P->fftD, dr, first, P->accb.as<float>(), g.spc_eff);
-        } else if (g.path == 2 && P->rot_tc) {
-            RotTcParams rp{};
-            rp.T = P->T.as<float2>(); rp.spc = g.spc; rp.spc_eff = g.spc_eff; rp.bs = g.bs; rp.R = g.R;
-            rp.first = first | (last ? 2 : 0);
-            rp.n_cblk = (g.spc + kRotTcW - 1) / kRotTcW;
-            rp.n_items = n * rp.n_cblk;
-            rp.twD = P->fftD.tw; rp.A = P->rotA.as<uint8_t>(); rp.a_bytes = P->rtcABytes;
-            rp.slots = a.d_slots; rp.drift = dr; rp.acc = P->accb.as<float>(); rp.win = P->winb.as<uint16_t>();
-            int sl = P->mma_scale_log2;
-            if (sl == 127) sl = dtype == ACQ_CI16 ? -10 : dtype == ACQ_CI8 ? -2 : 0;
-            rp.scale = std::ldexp(1.0f, sl);
-            rp.err = P->errflag.as<int>();
-            int sms = 1;
-            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P->device));
-            klog(P, (const void*)P->rot_tc, "k_rot_tc");
-            P->rot_tc<<<std::max(1, std::min(sms, rp.n_items)), kRotTcThreads, P->smem_rtc, st>>>(rp);
         } else if (g.path == 2 && P->rot_mma) {
             RotMmaParams rp{};
             rp.T = P->T.as<float2>(); rp.spc = g.spc; rp.spc_eff = g.spc_eff; rp.bs = g.bs; rp.R = g.R;
@@ -2078,11 +2006,6 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             const int n_cand = g.R * (1 << (g.ndb - 1));
             if (value != ACQ_PREC_FP32 && g.path == 2 && g.n_be == 1 && n_cand <= 32 && !getenv_flag("ACQ_GENERIC_FFT"))
                 fn = pick_rot_mma(g.n_coh, g.nb, n_cand, 1 << (g.ndb - 1), static_cast<int>(value), &smem);
-            RotTcFn tc = nullptr;
-            if (value == ACQ_PREC_FP16_SPLIT && g.path == 2 && g.n_be == 1 && !getenv_flag("ACQ_GENERIC_FFT") &&
-                !getenv_flag("ACQ_NO_ROT_TC"))
-                tc = setup_rot_tc(P);
-            if (tc) fn = nullptr;
             if (fn) {
                 set_smem((const void*)fn, smem);
                 P->errflag.ensure(sizeof(int));
@@ -2090,8 +2013,7 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             }
             P->rot_mma = fn;
             P->smem_mma = smem;
-            P->rot_tc = tc;
-            P->rot_prec = (fn || tc) ? static_cast<int>(value) : ACQ_PREC_FP32;
+            P->rot_prec = fn ? static_cast<int>(value) : ACQ_PREC_FP32;
             if (effective) *effective = P->rot_prec;
             return;
         }

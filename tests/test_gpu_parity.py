@@ -416,7 +416,7 @@ def test_rotation_workload_geometry_all_precisions(n_nc):
     outs = _oracles("GPSL5I", 20e6, prns, _complex(sig), **kw)
     plan = A.plan_acquire(A.GPSL5I(), 20e6, prns, **kw)
     assert (plan.num_doppler_bins, plan.geometry.num_blocks, plan.num_secondary_rotations) == (500, 25, 10)
-    for prec, kernel in [("fp32", "k_col_rot_sb<20,25,8>"), ("fp16_split", "k_rot_tc<20,25,2>"),
+    for prec, kernel in [("fp32", "k_col_rot_sb<20,25,8>"), ("fp16_split", "k_rot_mma<20,25,24,2,fp16,2>"),
                          ("bf16_split", "k_rot_mma<20,25,24,2,bf16,2>")]:
         assert plan.set_rotation_precision(prec) == prec
         res = A.acquire_b(plan, sig, prns, store_power_bins=True)

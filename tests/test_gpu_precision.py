@@ -62,7 +62,6 @@ def test_tensor_core_combine(case, prec):
     assert plan.set_rotation_precision(prec) == prec
     try:
         res = A.acquire_b(plan, sig, c["prns"], store_power_bins=True)
-        print(f"{name} {prec}: {[k for k in plan.last_kernels() if 'rot' in k]}")
     finally:
         plan.set_rotation_precision("fp32")
     for r, b in zip(res, base):
