@@ -98,29 +98,70 @@ class GlobalMeanNoiseEstimator(AbstractNoiseEstimator):
 
 
 # ---------------------------------------------------------------- results
-@dataclass
+class _Shared:
+    """Fields every result of one request shares (the plan's system and geometry)."""
+    __slots__ = ("system", "sampling_frequency", "dopplers", "num_blocks", "block_size", "num_secondary_rotations")
+
+    def __init__(self, system, sampling_frequency, dopplers, num_blocks, block_size, num_secondary_rotations):
+        self.system, self.sampling_frequency, self.dopplers = system, sampling_frequency, dopplers
+        self.num_blocks, self.block_size, self.num_secondary_rotations = num_blocks, block_size, num_secondary_rotations
+
+
 class AcquisitionResults:
-    system: GNSSSystem
-    prn: int
-    sampling_frequency: float
-    carrier_doppler: float
-    code_phase: float
-    secondary_code_phase: Optional[int]
-    CN0: float
-    noise_power: np.float32
-    peak_to_noise_ratio: np.float32
-    num_noncoherent_integrations: int
-    power_bins: Optional[np.ndarray]
-    dopplers: np.ndarray
-    num_blocks: int
-    block_size: int
-    num_secondary_rotations: int
-    # decision indices reported by the GPU pipeline (0-based)
-    peak_power: np.float32 = np.float32(0)
-    peak_doppler_bin: int = 0
-    peak_code_bin: int = 0
-    sign_pattern: int = -1
-    bit_edge: int = -1
+    """One acquisition result (src/Acquisition.jl:81-109) plus the decision indices the GPU pipeline
+    reports (0-based). The values are read from the request's own copy of the C result records,
+    so a later acquisition on the plan leaves them unchanged; ``power_bins`` is the plan's cached
+    per-PRN buffer, overwritten by the next acquisition that stores power bins (the reference's
+    aliasing, test/plan.jl:350-355)."""
+    __slots__ = ("_a", "_i", "_s", "power_bins")
+    _FIELDS = ("system", "prn", "sampling_frequency", "carrier_doppler", "code_phase", "secondary_code_phase", "CN0",
+               "noise_power", "peak_to_noise_ratio", "num_noncoherent_integrations", "power_bins", "dopplers",
+               "num_blocks", "block_size", "num_secondary_rotations", "peak_power", "peak_doppler_bin",
+               "peak_code_bin", "sign_pattern", "bit_edge")
+
+    def __init__(self, records, index, shared, power_bins=None):
+        self._a, self._i, self._s, self.power_bins = records, index, shared, power_bins
+
+    def _f(self, name):
+        return self._a[name][self._i]
+
+    system = property(lambda self: self._s.system)
+    sampling_frequency = property(lambda self: self._s.sampling_frequency)
+    dopplers = property(lambda self: self._s.dopplers)
+    num_blocks = property(lambda self: self._s.num_blocks)
+    block_size = property(lambda self: self._s.block_size)
+    num_secondary_rotations = property(lambda self: self._s.num_secondary_rotations)
+    prn = property(lambda self: int(self._f("prn")))
+    carrier_doppler = property(lambda self: float(self._f("carrier_doppler_hz")))
+    code_phase = property(lambda self: float(self._f("code_phase")))
+    CN0 = property(lambda self: float(self._f("cn0_dbhz")))
+    noise_power = property(lambda self: np.float32(self._f("noise_power")))
+    peak_to_noise_ratio = property(lambda self: np.float32(self._f("peak_to_noise_ratio")))
+    peak_power = property(lambda self: np.float32(self._f("peak_power")))
+    num_noncoherent_integrations = property(lambda self: int(self._f("num_noncoherent_integrations")))
+    peak_doppler_bin = property(lambda self: int(self._f("peak_doppler_bin")))
+    peak_code_bin = property(lambda self: int(self._f("peak_code_bin")))
+    sign_pattern = property(lambda self: int(self._f("sign_pattern")))
+    bit_edge = property(lambda self: int(self._f("bit_edge")))
+
+    @property
+    def secondary_code_phase(self) -> Optional[int]:
+        v = int(self._f("secondary_code_phase"))
+        return None if v < 0 else v
+
+    def __eq__(self, other):
+        if not isinstance(other, AcquisitionResults):
+            return NotImplemented
+        for f in self._FIELDS:
+            a, b = getattr(self, f), getattr(other, f)
+            if isinstance(a, np.ndarray) or isinstance(b, np.ndarray):
+                if not (a is b or (a is not None and b is not None and np.array_equal(a, b))):
+                    return False
+            elif a != b:
+                return False
+        return True
+
+    __hash__ = None
 
     def __repr__(self):
         return (f"AcquisitionResults: PRN {self.prn}, CN0 = {self.CN0:.2f} dB-Hz, Doppler = "
@@ -347,28 +388,21 @@ assert _RESULT_DTYPE.itemsize == C.sizeof(L.Result)
 
 
 def _results(plan: AcquisitionPlan, res_arr, prns, store_power_bins, bins):
-    """AcquisitionResults from the C result records (a ctypes array of Result, or a structured
-    numpy view of one; columns are pulled in bulk)."""
+    """AcquisitionResults over the C result records (a ctypes array of Result, or a structured numpy
+    view of one), which this request owns: the records are read when a field is accessed."""
     g = plan.geometry
     a = res_arr if isinstance(res_arr, np.ndarray) else np.frombuffer(res_arr, dtype=_RESULT_DTYPE, count=len(prns))
-    prn, sec = a["prn"].tolist(), a["secondary_code_phase"].tolist()
-    dop, cp, cn0 = a["carrier_doppler_hz"].tolist(), a["code_phase"].tolist(), a["cn0_dbhz"].tolist()
-    npow, pnr, ppow = a["noise_power"].copy(), a["peak_to_noise_ratio"].copy(), a["peak_power"].copy()
-    nnc, pdb, pcb = a["num_noncoherent_integrations"].tolist(), a["peak_doppler_bin"].tolist(), a["peak_code_bin"].tolist()
-    sgn, edge = a["sign_pattern"].tolist(), a["bit_edge"].tolist()
+    shared = _Shared(plan.system, plan.sampling_freq, plan.doppler_freqs, g.num_blocks, g.block_size,
+                     g.num_secondary_rotations)
+    if not store_power_bins:
+        return [AcquisitionResults(a, i, shared) for i in range(len(prns))]
     out = []
     for i, p in enumerate(prns):
-        pb = None
-        if store_power_bins:
-            slot = plan.avail_prns.index(p)
-            if plan.result_buffers[slot] is None:
-                plan.result_buffers[slot] = np.empty((g.num_doppler_bins, g.samples_per_code_eff), np.float32)
-            np.copyto(plan.result_buffers[slot], bins[i])
-            pb = plan.result_buffers[slot]
-        out.append(AcquisitionResults(
-            plan.system, prn[i], plan.sampling_freq, dop[i], cp[i], None if sec[i] < 0 else sec[i], cn0[i],
-            npow[i], pnr[i], nnc[i], pb, plan.doppler_freqs, g.num_blocks, g.block_size,
-            g.num_secondary_rotations, ppow[i], pdb[i], pcb[i], sgn[i], edge[i]))
+        slot = plan.avail_prns.index(p)
+        if plan.result_buffers[slot] is None:
+            plan.result_buffers[slot] = np.empty((g.num_doppler_bins, g.samples_per_code_eff), np.float32)
+        np.copyto(plan.result_buffers[slot], bins[i])
+        out.append(AcquisitionResults(a, i, shared, plan.result_buffers[slot]))
     return out
 
 
