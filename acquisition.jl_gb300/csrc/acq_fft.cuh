@@ -53,6 +53,15 @@ __device__ __forceinline__ float2 c_scale(float2 a, float s) {
         : "f"(a.x), "f"(a.y), "f"(s));
     return r;
 }
+// a + s * y with one rounding per component (packed fused multiply-add)
+__device__ __forceinline__ float2 c_axpy(float s, float2 y, float2 a) {
+    float2 r;
+    asm("{.reg .b64 rs, ry, ra, rd;\n\tmov.b64 rs, {%2, %2};\n\tmov.b64 ry, {%3, %4};\n\t"
+        "mov.b64 ra, {%5, %6};\n\tfma.rn.f32x2 rd, rs, ry, ra;\n\tmov.b64 {%0, %1}, rd;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(s), "f"(y.x), "f"(y.y), "f"(a.x), "f"(a.y));
+    return r;
+}
 __device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

@@ -983,9 +983,7 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
                     for (int p = 0; p < NC; ++p) {
                         int row = base + NB * p;
                         if (row >= ND) row -= ND;
-                        const float sg = pq[p];
-                        const float2 x = tile[row * W + t1];
-                        v[p] = make_float2(sg * x.x, sg * x.y);
+                        v[p] = c_scale(tile[row * W + t1], pq[p]);
                     }
                     RegFFT<NC, false>::run(v);
                     static_for<0, NC>([&](auto kc) {
@@ -1003,15 +1001,30 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
 #pragma unroll
                     for (int m = 0; m < NB; ++m) v[m] = wk[(NB * k1 + m) * W + t2];
                     RegFFT<NB, false>::run(v);
-                    static_for<0, NB>([&](auto kc) {
-                        constexpr int k2 = decltype(kc)::value;
-                        constexpr int pr = reg_perm(NB, k2);
-                        const float2 x = v[pr];
-                        const float pw = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
-                        const bool take = !use_max || pw > best[k2];
-                        best[k2] = take ? pw : best[k2];
-                        bwin[k2] = take ? cand : bwin[k2];
-                    });
+                    // block-uniform cases: a single candidate per rotation, or a max whose winners
+                    // are kept only on the last step (the only winner map that survives)
+                    if (!use_max) {
+                        static_for<0, NB>([&](auto kc) {
+                            constexpr int k2 = decltype(kc)::value;
+                            const float2 x = v[reg_perm(NB, k2)];
+                            best[k2] = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+                        });
+                    } else if (!(first & 2)) {
+                        static_for<0, NB>([&](auto kc) {
+                            constexpr int k2 = decltype(kc)::value;
+                            const float2 x = v[reg_perm(NB, k2)];
+                            best[k2] = fmaxf(best[k2], __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
+                        });
+                    } else {
+                        static_for<0, NB>([&](auto kc) {
+                            constexpr int k2 = decltype(kc)::value;
+                            const float2 x = v[reg_perm(NB, k2)];
+                            const float pw = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+                            const bool take = pw > best[k2];
+                            best[k2] = take ? pw : best[k2];
+                            bwin[k2] = take ? cand : bwin[k2];
+                        });
+                    }
                 }
                 __syncthreads();
             }
@@ -1125,21 +1138,28 @@ __global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W, ((1 << (NDB - 1)) *
 #pragma unroll
                 for (int b = 0; b < NDB; ++b) {
                     const float2 y = wk[b * ND * W + (N2 * k1 + m) * W + t2];
-                    a = b == 0 ? make_float2(s[0] * y.x, s[0] * y.y) : make_float2(a.x + s[b] * y.x, a.y + s[b] * y.y);
+                    a = b == 0 ? c_scale(y, s[0]) : c_axpy(s[b], y, a);
                 }
                 v[m] = a;
             }
             RegFFT<N2, false>::run(v);
             const int cand = e * NP + p2;
-            static_for<0, N2>([&](auto kc) {
-                constexpr int k2 = decltype(kc)::value;
-                constexpr int pr = reg_perm(N2, k2);
-                const float2 x = v[pr];
-                const float pw = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
-                const bool take = pw > best[k2];
-                best[k2] = take ? pw : best[k2];
-                bwin[k2] = take ? cand : bwin[k2];
-            });
+            if (first & 2) {   // the last step's winners are stored
+                static_for<0, N2>([&](auto kc) {
+                    constexpr int k2 = decltype(kc)::value;
+                    const float2 x = v[reg_perm(N2, k2)];
+                    const float pw = __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y));
+                    const bool take = pw > best[k2];
+                    best[k2] = take ? pw : best[k2];
+                    bwin[k2] = take ? cand : bwin[k2];
+                });
+            } else {           // earlier steps only add the maxima
+                static_for<0, N2>([&](auto kc) {
+                    constexpr int k2 = decltype(kc)::value;
+                    const float2 x = v[reg_perm(N2, k2)];
+                    best[k2] = fmaxf(best[k2], __fadd_rn(__fmul_rn(x.x, x.x), __fmul_rn(x.y, x.y)));
+                });
+            }
         }
         __syncthreads();
     }

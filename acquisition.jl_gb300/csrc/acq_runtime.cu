@@ -755,7 +755,14 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
         }
     if (!fn || (g.spc % 2) != 0) return;
     const size_t tall = sizeof(float2) * (size_t)g.n_nc * n_prns * g.ndop * g.spc;
-    size_t cap = 4ull << 30;   // all-steps tile buffer per plan (batches hold many plans)
+    // all-steps tile buffer per plan: up to 16 GB and an eighth of the device's memory (batches hold
+    // many plans); larger requests run the per-step column kernels
+    size_t cap = 16ull << 30;
+    {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) cap = std::min(cap, total_b / 8);
+        else cudaGetLastError();
+    }
     if (const char* e = std::getenv("ACQ_TALL_CAP_GB")) cap = static_cast<size_t>(std::atof(e) * (1ull << 30));
     if (tall > cap) return;
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
