@@ -464,6 +464,7 @@ __global__ void k_extract(const float* __restrict__ acc, const uint16_t* __restr
                           ExtractParams P, acq_result* __restrict__ res) {
     __shared__ double dred[256];
     __shared__ unsigned long long kred[256];
+    pdl_wait();
     const int pi = blockIdx.x;
     unsigned long long best = 0ULL;
     for (int i = threadIdx.x; i < P.npk; i += blockDim.x) {

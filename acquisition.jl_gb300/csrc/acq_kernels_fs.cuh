@@ -13,6 +13,14 @@
 
 namespace acq {
 
+// Programmatic dependent launch (a kernel launched with programmatic stream serialisation may
+// start while its predecessor in the stream finishes): pdl_trigger lets the next kernel's blocks
+// be scheduled once every block of this grid has issued it; pdl_wait blocks until the preceding
+// grid has completed and its memory operations are visible. Every kernel of such a chain waits
+// before it exits, so the ordering stays transitive. Both are no-ops in a normal launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ------------------------------------------------------------------ specialised hot sizes
 __host__ __device__ constexpr int tile_row_pitch(int n2) { return n2 % 2 == 0 ? n2 + 1 : n2; }
 
@@ -409,6 +417,7 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
     int* rowof = sht + p.n_nc * N2;                          // N2: destination row of output k2
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smraw) + ((2 * BS * 8 + N2 * AW * 4 + (p.n_nc + 1) * N2 * 4 + 15) / 8);
     const uint32_t tile_bytes = static_cast<uint32_t>(N2) * W * 8;
+    pdl_trigger();
     if (threadIdx.x == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
@@ -416,6 +425,7 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
     }
     for (int i = threadIdx.x; i < N2 * AW; i += blockDim.x) accs[i] = 0.f;
     __syncthreads();
+    pdl_wait();   // the tile and the zeroed accumulator edges
     const int n_items = p.n_items;   // = n_req * n1 * n_cblk, item = (pi * n1 + k1) * n_cblk + cb
     const int my_items = n_items > static_cast<int>(blockIdx.x)
                              ? (n_items - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1

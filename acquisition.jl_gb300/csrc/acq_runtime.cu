@@ -139,6 +139,8 @@ __global__ void k_gather_cols(const float* __restrict__ in, int64_t rows, int64_
 __global__ void k_edge_peaks(const float* __restrict__ acc, int ndop, int spc, int spc_eff, int W, int H, int n_bound,
                              int slot0, int npk, unsigned long long* __restrict__ peakpart) {
     __shared__ unsigned long long kred[8];
+    pdl_trigger();
+    pdl_wait();
     const int j = blockIdx.x, pi = blockIdx.y;
     const int b = j == n_bound - 1 ? spc : j * W;
     const float* ap = acc + static_cast<int64_t>(pi) * ndop * spc_eff;
@@ -171,6 +173,7 @@ __global__ void k_edge_peaks(const float* __restrict__ acc, int ndop, int spc, i
 // stored by exactly one work item, so the accumulator needs no full clear.
 __global__ void k_zero_edges(float* __restrict__ acc, int64_t rows, int spc, int spc_eff, int W, int H,
                              int n_bound) {
+    pdl_trigger();
     const int per_row = n_bound * 2 * H;
     const int64_t total = rows * per_row;
     for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < total;
@@ -184,6 +187,7 @@ __global__ void k_zero_edges(float* __restrict__ acc, int64_t rows, int spc, int
         if (c >= spc) c -= spc;
         ACQ_BC(&acc[r * spc_eff + c], 22) acc[r * spc_eff + c] = 0.f;
     }
+    pdl_wait();   // nothing here reads the tile; the wait keeps the chain's ordering transitive
 }
 
 #ifdef ACQ_BOUNDS_CHECK
@@ -537,6 +541,23 @@ void t_end(acq_plan* P) {
     if (!P->timing) return;
     CK(cudaEventRecord(P->ev_stop[P->ev_used], P->stream));
     ++P->ev_used;
+}
+
+// Launch with programmatic stream serialisation when `pdl` is set (the kernel may start while the
+// previous kernel of the stream finishes; it calls pdl_wait before using that kernel's results).
+template <typename... KArgs, typename... Args>
+void launch(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = pdl ? attr : nullptr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    CK(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
 }
 
 // Launch log: the kernel about to be launched (a size-specialised kernel by its registered name).
@@ -1094,6 +1115,15 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     // the TMA path, one launch per step otherwise)
     const bool use_tmma = use_tma && P->tmma;
     const bool use_tmma_step = !use_fused && !use_tma && P->tmma;
+    // the all-steps tensor-core chain (operand blocks -> tile -> edge zeroing -> Doppler-group column
+    // stage -> edge keys -> extraction) overlaps each kernel's launch with its predecessor's tail;
+    // not while the kernels are timed one by one. Only for steps whose tile is small (at most
+    // 256 MB): there the launch gaps are a visible share of the step (1 ms, 32 PRNs at 4 MHz:
+    // +3 % acquisitions/s); on multi-GB tiles the early-resident blocks cost more than the gaps
+    // (10 ms x 8 at 5 MHz: -1.3 %)
+    const size_t step_tile_bytes = sizeof(float2) * (size_t)g.n_nc * P->prns.size() * g.ndop * g.spc;
+    const bool pdl = use_tmma && P->col_k1 && !P->timing && step_tile_bytes <= (256ull << 20) &&
+                     !getenv_flag("ACQ_NO_PDL");
     if (!use_tmma && !use_tmma_step) {
         t_begin(P, ACQ_KERNEL_FRONTEND);
         klog(P, nullptr, "k_frontend");
@@ -1148,7 +1178,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         tp.err = P->errflag.as<int>();
         t_begin(P, ACQ_KERNEL_TILE);
         klog(P, nullptr, "k_tile_mma");
-        k_tile_mma<<<tp.n_chunks * tp.cpc, kTmmaThreads, P->smem_tmma, st>>>(tp);
+        launch(pdl, k_tile_mma, dim3(tp.n_chunks * tp.cpc), dim3(kTmmaThreads), P->smem_tmma, st, tp);
         t_end(P);
         ++L;
     }
@@ -1180,8 +1210,8 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             const int64_t rows = static_cast<int64_t>(n) * g.ndop;
             const int64_t total = rows * n_bound * 2 * P->tmaH;
             klog(P, nullptr, "k_zero_edges");
-            k_zero_edges<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
-                P->accb.as<float>(), rows, g.spc, g.spc_eff, wc, P->tmaH, n_bound);
+            launch(pdl, k_zero_edges, dim3(static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096))),
+                   dim3(256), 0, st, P->accb.as<float>(), rows, g.spc, g.spc_eff, wc, P->tmaH, n_bound);
             ++L;
         }
         ColTmaParams cp{};
@@ -1202,15 +1232,15 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             cp.npk = g.n_coh * cp.n_cblk + (P->tmaH > 0 ? n_bound : 0);
             const int grid = std::max(1, std::min(P->k1Grid, cp.n_items));
             klog(P, (const void*)P->col_k1, "k_col_tma_k1");
-            P->col_k1<<<grid, 128, P->smem_col_k1, st>>>(P->tmapK1, cp);
+            launch(pdl, P->col_k1, dim3(grid), dim3(128), P->smem_col_k1, st, P->tmapK1, cp);
             t_end(P);
             ++L;
             if (P->tmaH > 0) {
                 t_begin(P, ACQ_KERNEL_STATS);
                 klog(P, nullptr, "k_edge_peaks");
-                k_edge_peaks<<<dim3(n_bound, n), 128, 0, st>>>(P->accb.as<float>(), g.ndop, g.spc, g.spc_eff, P->k1W,
-                                                              P->tmaH, n_bound, g.n_coh * cp.n_cblk, cp.npk,
-                                                              P->peakpart.as<unsigned long long>());
+                launch(pdl, k_edge_peaks, dim3(n_bound, n), dim3(128), 0, st, P->accb.as<float>(), g.ndop, g.spc,
+                       g.spc_eff, P->k1W, P->tmaH, n_bound, g.n_coh * cp.n_cblk, cp.npk,
+                       P->peakpart.as<unsigned long long>());
                 t_end(P);
                 ++L;
             }
@@ -1371,9 +1401,9 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     EP.doppler_first = g.doppler_first; EP.doppler_step = g.doppler_step; EP.cfar_thr = g.cfar_thr;
     t_begin(P, ACQ_KERNEL_EXTRACT);
     klog(P, nullptr, "k_extract");
-    k_extract<<<n, kThreads, 0, st>>>(P->accb.as<float>(), P->winb.as<uint16_t>(), P->rowpart.as<double>(),
-                                      P->colsum.as<double>(), P->peakpart.as<unsigned long long>(), a.d_prn_ids,
-                                      EP, a.d_res);
+    launch(pdl && stats_npk > 0, k_extract, dim3(n), dim3(kThreads), 0, st, P->accb.as<float>(),
+           P->winb.as<uint16_t>(), P->rowpart.as<double>(), P->colsum.as<double>(),
+           P->peakpart.as<unsigned long long>(), a.d_prn_ids, EP, a.d_res);
     t_end(P);
     ++L;
     if (g.R > 1) {

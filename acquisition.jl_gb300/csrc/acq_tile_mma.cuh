@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __r
                                                                  float* __restrict__ inv_scale) {
     __shared__ __align__(16) uint16_t xh[4][kTmmaMaxSpan];
     __shared__ float red[kTmmaStubThreads / 32];
+    pdl_trigger();
     const int rho = blockIdx.x, step = blockIdx.y;
     const int tid = threadIdx.x;
     const int64_t seg0 = static_cast<int64_t>(step) * seg_len;
@@ -263,6 +264,7 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
+    pdl_wait();   // the operand blocks and their scales (code rows and slots are already in place)
 
     if (warp == kTmmaDrainWarps) {
         if (lane == 0) {
@@ -386,6 +388,9 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
             if (!ok) break;
         }
     }
+    // the next kernel's blocks may be scheduled once every block here has finished its work (an
+    // earlier trigger would let them take shared memory beside blocks that still drain)
+    pdl_trigger();
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
