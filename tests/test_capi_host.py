@@ -32,6 +32,17 @@ def test_library_exports_every_header_symbol():
     assert b"sm_103a" in L.load().acq_version()
 
 
+def test_python_option_constants_match_the_header():
+    header = open(os.path.join(ROOT, "include", "acqgb300.h")).read()
+    defines = dict(re.findall(r"#define (ACQ_(?:OPT|TILE|FORM|PREC)_\w+)\s+(-?\d+)", header))
+    from acqgb300 import api
+    for name, val in defines.items():
+        if name.startswith("ACQ_PREC_"):
+            assert api.PRECISIONS[name[len("ACQ_PREC_"):].lower()] == int(val), name
+        else:
+            assert getattr(L, name) == int(val), name
+
+
 def test_result_struct_layout():
     assert C.sizeof(L.Result) == 72
     assert C.sizeof(L.PlanDesc) == 56
