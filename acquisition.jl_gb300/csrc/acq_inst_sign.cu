@@ -51,13 +51,23 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
                      "k_col_sign_sb<" #N1 "," #N2 "," #W "," #NDB ">");                              \
     }
 
+// two data bits: the half-spectrum form (same block shape and shared memory as k_col_sign_sb)
+#define ACQ_SFOLD_CASE(N1, N2, W)                                                                    \
+    if (ndop == N1 * N2 && ndb == 2 && (want_w == 0 || want_w == W)) {                                \
+        *w = W;                                                                                      \
+        *threads = 2 * N1 * W;                                                                       \
+        *smem = sizeof(float2) * ((size_t)3 * N1 * N2 * W + N1 * N2) + 64;                            \
+        return named(&k_col_sign_fold<N1, N2, W>, "k_col_sign_fold<" #N1 "," #N2 "," #W ">");        \
+    }
+
 SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {
     // columns per block: the first instantiation listed for the size (ndop 800: four columns, two
     // CTAs per SM, 5.81 ms vs 6.29 ms with eight on the 40 ms x 2 search), or ACQ_SIGN_W when set
     const char* e = std::getenv("ACQ_SIGN_W");
     const int want_w = e ? std::atoi(e) : 0;
-    ACQ_SSB_CASE(32, 25, 4, 2) ACQ_SSB_CASE(32, 25, 8, 2) ACQ_SSB_CASE(32, 20, 8, 2) ACQ_SSB_CASE(32, 40, 4, 2) ACQ_SSB_CASE(20, 20, 8, 2)
-    ACQ_SSB_CASE(16, 25, 8, 1) ACQ_SSB_CASE(20, 10, 16, 2)
+    ACQ_SFOLD_CASE(32, 25, 4) ACQ_SFOLD_CASE(32, 25, 8) ACQ_SFOLD_CASE(32, 20, 8) ACQ_SFOLD_CASE(32, 40, 4)
+    ACQ_SFOLD_CASE(20, 20, 8) ACQ_SFOLD_CASE(20, 10, 16)
+    ACQ_SSB_CASE(16, 25, 8, 1)
     return nullptr;
 }
 

@@ -1207,4 +1207,173 @@ __global__ void __launch_bounds__((1 << (NDB - 1)) * N1 * W, ((1 << (NDB - 1)) *
     scatter_rmw<W>(stg, wst, ND * W, tid, blockDim.x, wv, c0, spc, spc_eff, 0, drift, first, ap, wp);
 }
 
+// ------------------------------------------------------------------ bit-edge search by half spectra
+// The search of k_col_sign_sb for two data bits (src/noncoherent_integration.jl:60-115 with the
+// patterns of src/sign_patterns.jl:23-47, s(p, 1) = +-s(p, 0)), with less work. Candidate (e, p)
+// of a column is |DFT_ND(f)|^2, f[i] = s(p, 0) x[o + i] + s(p, 1) x[o + SUB + i] for i < SUB =
+// ND / 2 and 0 beyond, o = e * edge_step (each sub-block is placed at the start of its own
+// zero-padded transform). From one edge to the next f moves by a cyclic shift when
+// s(p, 0) = s(p, 1) and by a negacyclic one (the wrapped part negated) when s(p, 0) = -s(p, 1).
+// The even bins are DFT_SUB(f), whose power a cyclic shift leaves unchanged; the odd bins are
+// DFT_SUB(f W_ND^i), whose power a negacyclic shift leaves unchanged. So each pattern has one half
+// spectrum that is the same for every edge (computed once, as edge 0: the first candidate wins
+// exact ties) and one computed per edge: 2 (1 + n_be) half spectra per column instead of
+// 4 n_be, 37.5 % fewer transform points at four edges.
+// Half spectrum of parity q in the split n = n2 + N2 n1 (n1 < N1 / 2 nonzero), k = k1 + N1 k2,
+// k1 = 2 j + q: pass 1 = DFT_{N1/2} over n1 of f[n2 + N2 n1] W_N1^(q n1), times W_ND^(n2 k1);
+// pass 2 = DFT_N2 over n2 for each k1 of that parity.
+// Thread (g, k1, t) owns bins k1 + N1 k2 of column t and takes units g, g + 2, ... of its
+// parity's list [the edge-invariant half, edges 0 .. n_be - 1]; each round transforms two units of
+// each parity. The two groups' maxima merge in candidate order (e, p), as in k_col_sign_sb.
+template <int N1, int N2, int W>
+__global__ void __launch_bounds__(2 * N1 * W, (2 * N1 * W <= 256) ? 2 : 1)
+    k_col_sign_fold(const float2* __restrict__ T, int spc, const float2* __restrict__ twD,
+                    const float* __restrict__ pats, int n_coh, int n_be, int edge_step, const int* __restrict__ slots,
+                    const int* __restrict__ drift, int first, float* __restrict__ acc, uint16_t* __restrict__ win,
+                    int spc_eff) {
+    constexpr int ND = N1 * N2, SUB = ND / 2, H1 = N1 / 2, NP = 2;
+    static_assert(N1 % 2 == 0, "the half spectra split the pass-1 length");
+    extern __shared__ float2 sm[];
+    float2* tile = sm;
+    float2* wk = tile + ND * W;                 // 4 slots (parity, group) of SUB x W pass-1 results
+    float2* tws = wk + 2 * ND * W;
+    float* sgn = reinterpret_cast<float*>(tws + ND);   // s(p, b), NP x 2
+    const int tid = threadIdx.x;
+    const int pi = blockIdx.y;
+    const int slot = slots[pi];
+    const int c0 = blockIdx.x * W;
+    const int wv = min(W, spc - c0);
+    const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
+    {
+        // every load of the thread in flight at once, then the shared-memory stores
+        constexpr int NT = 2 * N1 * W, NL = (ND * W + NT - 1) / NT;
+        float2 tv[NL];
+#pragma unroll
+        for (int u = 0; u < NL; ++u) {
+            const int w = tid + u * NT;
+            const int e = w / W, t = w - (w / W) * W;
+            tv[u] = make_float2(0.f, 0.f);
+            if (w < ND * W && t < wv)
+                ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 45) tv[u] = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        }
+#pragma unroll
+        for (int u = 0; u < NL; ++u)
+            if (tid + u * NT < ND * W) tile[tid + u * NT] = tv[u];
+    }
+    for (int i = tid; i < ND; i += blockDim.x) tws[i] = twD[i];
+    if (tid < NP * 2) {
+        const int pp = tid / 2, b = tid - (tid / 2) * 2;
+        sgn[tid] = pats[(static_cast<int64_t>(slot) * NP + pp) * n_coh + b * (n_coh / 2)];
+    }
+    __syncthreads();
+    const int g = tid / (N1 * W), r2 = tid - g * (N1 * W);
+    const int k1 = r2 / W, t2 = r2 - (r2 / W) * W;
+    const int par = k1 & 1, jj = k1 >> 1;
+    const int p_cyc = sgn[0] == sgn[1] ? 0 : 1;   // the pattern whose even bins are edge-invariant
+    // (edge, pattern) of unit u of parity q
+    auto unit = [&](int q, int u, int& e, int& p) {
+        const int pinv = q == 0 ? p_cyc : 1 - p_cyc;
+        e = u == 0 ? 0 : u - 1;
+        p = u == 0 ? pinv : 1 - pinv;
+    };
+    float best[N2];
+    int bwin[N2];
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+        best[k2] = 0.f;
+        bwin[k2] = 0;
+    }
+    const int nu = n_be + 1;
+    for (int u0 = 0; u0 < nu; u0 += 2) {
+        // pass 1: slot s = 2 q + h holds unit u0 + h of parity q
+        for (int task = tid; task < 4 * N2 * W; task += blockDim.x) {
+            const int s = task / (N2 * W), r = task - s * (N2 * W);
+            const int q = s >> 1, u = u0 + (s & 1);
+            if (u >= nu) continue;
+            const int n2 = r / W, t = r - (r / W) * W;
+            int e, p;
+            unit(q, u, e, p);
+            const float s0 = sgn[p * 2], s1 = sgn[p * 2 + 1];
+            const int o = (e * edge_step) % ND;
+            float2 v[H1];
+#pragma unroll
+            for (int n1 = 0; n1 < H1; ++n1) {
+                int ra = o + n2 + N2 * n1;   // < ND + SUB
+                ra = ra >= ND ? ra - ND : ra;
+                int rb = ra + SUB;
+                rb = rb >= ND ? rb - ND : rb;
+                float2 y = c_axpy(s1, tile[rb * W + t], c_scale(tile[ra * W + t], s0));
+                if (q && n1 != 0) y = c_mul(y, tws[n1 * N2]);   // W_N1^n1
+                v[n1] = y;
+            }
+            RegFFT<H1, false>::run(v);
+            float2* x = wk + s * SUB * W;
+            static_for<0, H1>([&](auto kc) {
+                constexpr int j = decltype(kc)::value;
+                float2 y = v[reg_perm(H1, j)];
+                const int kk = 2 * j + q;
+                if (kk * n2 != 0) y = c_mul(y, tws[n2 * kk]);   // < ND
+                x[(n2 + N2 * j) * W + t] = y;
+            });
+        }
+        __syncthreads();
+        const int u = u0 + g;
+        if (u < nu) {
+            int e, p;
+            unit(par, u, e, p);
+            const int cand = e * NP + p;
+            const float2* x = wk + (2 * par + g) * SUB * W;
+            float2 v[N2];
+#pragma unroll
+            for (int m = 0; m < N2; ++m) v[m] = x[(m + N2 * jj) * W + t2];
+            RegFFT<N2, false>::run(v);
+            if (first & 2) {   // the last step's winners are stored; equal powers: the earlier candidate
+                static_for<0, N2>([&](auto kc) {
+                    constexpr int k2 = decltype(kc)::value;
+                    const float2 xv = v[reg_perm(N2, k2)];
+                    const float pw = __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y));
+                    const bool take = pw > best[k2] || (pw == best[k2] && cand < bwin[k2]);
+                    best[k2] = take ? pw : best[k2];
+                    bwin[k2] = take ? cand : bwin[k2];
+                });
+            } else {
+                static_for<0, N2>([&](auto kc) {
+                    constexpr int k2 = decltype(kc)::value;
+                    const float2 xv = v[reg_perm(N2, k2)];
+                    best[k2] = fmaxf(best[k2], __fadd_rn(__fmul_rn(xv.x, xv.x), __fmul_rn(xv.y, xv.y)));
+                });
+            }
+        }
+        __syncthreads();
+    }
+    // merge the two groups' maxima (candidate order (e, p)), stage, scatter
+    float* stg = reinterpret_cast<float*>(wk);
+    uint16_t* wst = reinterpret_cast<uint16_t*>(stg + 2 * ND * W);
+    constexpr int half = ND / 2;
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) {
+        const int om = k1 + N1 * k2;
+        const int row = om < half ? om + half : om - half;
+        stg[(g * ND + row) * W + t2] = best[k2];
+        wst[(g * ND + row) * W + t2] = static_cast<uint16_t>(bwin[k2]);
+    }
+    __syncthreads();
+    for (int w = tid; w < ND * W; w += blockDim.x) {
+        float bv = stg[w];
+        int bw = wst[w];
+        const float v = stg[ND * W + w];
+        const int c = wst[ND * W + w];
+        if (v > bv || (v == bv && c < bw)) {
+            bv = v;
+            bw = c;
+        }
+        stg[w] = bv;
+        wst[w] = static_cast<uint16_t>(bw);
+    }
+    __syncthreads();
+    float* ap = acc + static_cast<int64_t>(pi) * ND * spc_eff;
+    uint16_t* wp = win + static_cast<int64_t>(pi) * ND * spc_eff;
+    scatter_rmw<W>(stg, wst, ND * W, tid, blockDim.x, wv, c0, spc, spc_eff, 0, drift, first, ap, wp);
+}
+
 }  // namespace acq

@@ -398,7 +398,7 @@ def test_bit_edge_search_workload_geometry():
     assert plan.num_doppler_bins == 800 and plan.num_data_bits == 2
     res = A.acquire_b(plan, sig, prns, store_power_bins=True)
     ks = plan.last_kernels()
-    assert ks.count("k_col_sign_sb<32,25,4,2>") == 2, ks
+    assert ks.count("k_col_sign_fold<32,25,4>") == 2, ks
     _compare(res, _oracles("GPSL1CA", 5e6, prns, _complex(sig), **kw), "bit-edge-ndop800")
 
 
