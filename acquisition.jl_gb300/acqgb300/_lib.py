@@ -97,6 +97,7 @@ ACQ_OPT_TILE_ROWS = 9
 ACQ_OPT_TRANSFORM_LENGTH = 10
 ACQ_OPT_TILE_MMA = 11
 ACQ_OPT_COLUMN_WAIT_POLLS = 12
+ACQ_OPT_SEARCH_WIDTH, ACQ_OPT_SEARCH_SPLIT = 13, 14
 ACQ_FORM_FUSED, ACQ_FORM_PLAIN = 0, 1
 KERNEL_KINDS = 8
 KERNEL_NAMES = ["frontend", "tile", "column", "stats", "extract", "secondary", "fused", "k7"]

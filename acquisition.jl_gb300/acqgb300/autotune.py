@@ -12,6 +12,11 @@ accumulation sums (results within FP32 rounding, decisions unchanged):
   form                 ACQ_OPT_FORM                plain (one kernel per stage) or fused (cluster)
   tile_mma             ACQ_OPT_TILE_MMA            coherent tile as a tensor-core correlation GEMM (1) or
                                                    FP32 FFTs (0); results within FP32 rounding
+  search_width         ACQ_OPT_SEARCH_WIDTH        code-phase columns per bit-edge / rotation search CTA
+  search_split         ACQ_OPT_SEARCH_SPLIT        FFT split of the bit-edge search (first-pass length;
+                                                   the radix structure of its register FFTs)
+A candidate the plan's sizes have no instantiation for reads back a different value and is
+skipped.
 Reduced-precision rotation combines change results within their stated bounds, so they are
 tuned only on request (``allow_reduced_precision``).
 
@@ -38,6 +43,8 @@ KNOBS = {
     "column_width": L.ACQ_OPT_COLUMN_WIDTH,
     "column_ctas_per_sm": L.ACQ_OPT_COLUMN_CTAS_PER_SM,
     "tile_mma": L.ACQ_OPT_TILE_MMA,
+    "search_width": L.ACQ_OPT_SEARCH_WIDTH,
+    "search_split": L.ACQ_OPT_SEARCH_SPLIT,
 }
 # knobs whose 0 is a setting (for the others 0 means the plan's sizes lack that kernel)
 ZERO_IS_A_VALUE = {"tile_mma"}
@@ -51,7 +58,7 @@ def candidates(plan) -> dict:
     rows = [1, 2] if plan.geometry.num_coherently_integrated_code_periods >= 2 else [1]
     return {"tile_rows": rows, "tile_threads": [64, 128, 192, 256], "tile_blocks": blocks, "tile_pad": [0, 1, 9],
             "column_width": [8, 12, 16, 20, 24, 32, 64, 128, 256], "column_ctas_per_sm": [1, 2, 3, 4, 6], "form": ["plain", "fused"],
-            "tile_mma": [1, 0]}
+            "tile_mma": [1, 0], "search_width": [2, 4, 8, 16], "search_split": [20, 25, 32, 40]}
 
 
 def current(plan) -> dict:
@@ -160,6 +167,10 @@ def tune(plan, signal_dev, prns, *, reps: int = 3, passes: int = 2, cache: str |
     def cost(settings):
         eff = apply(plan, settings)
         if any(v is None for v in eff.values()):
+            return float("inf")
+        # a value the plan's sizes have no instantiation for (the option kept another)
+        if any(k in KNOBS and k not in ZERO_IS_A_VALUE and settings[k] and eff.get(k) != settings[k]
+               for k in settings):
             return float("inf")
         acquire_device(plan, signal_dev, prns)   # warm-up (and smem limits)
         ts = []

@@ -38,13 +38,16 @@ using RotSbFn = void (*)(const float2*, int, const float2*, const float*, int, i
                          const int*, int, float*, uint16_t*, int);
 // rotation stage split by (coherent periods, blocks per period); nullptr when not instantiated.
 // *w = columns per block, *threads = block size.
-RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads);
+// want_w: columns per CTA wanted (0: the default for the size); *w, *threads: the kernel's shape
+RotSbFn pick_rot_sb(int n_coh, int nb, int want_w, int* w, int* threads);
 
 using SignSbFn = void (*)(const float2*, int, const float2*, const float*, int, int, int, const int*, const int*, int,
                           float*, uint16_t*, int);
 // data-bit / bit-edge search split by sub-blocks for (ndop, data bits); nullptr when not
 // instantiated. *w = columns per block, *threads = block size, *smem = dynamic bytes.
-SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem);
+// want_w / want_n1: columns per CTA and first-pass length of the FFT split wanted (0: the default
+// for the size, the first instantiation listed); *w, *n1, *threads, *smem: the kernel's shape
+SignSbFn pick_sign_sb(int ndop, int ndb, int want_w, int want_n1, int* w, int* n1, int* threads, size_t* smem);
 
 struct RotMmaParams;
 struct DftMmaParams;

@@ -26,8 +26,15 @@ RotFsFn pick_rot_fs(int ndop) {
     }
 }
 
+// W = 16 for tiles up to 384 rows, 8 above (the default); ACQ_RSB_W_CASE adds another width
+#define ACQ_RSB_W_CASE(NC, NB, W)                                           \
+    if (n_coh == NC && nb == NB && want_w == W) {                           \
+        *w = W;                                                             \
+        *threads = rot_sb_block(NC, NB, W);                                 \
+        return named(&k_col_rot_sb<NC, NB, W>, "k_col_rot_sb<" #NC "," #NB "," #W ">"); \
+    }
 #define ACQ_RSB_CASE(NC, NB)                                                \
-    if (n_coh == NC && nb == NB) {                                          \
+    if (n_coh == NC && nb == NB && (want_w == 0 || want_w == ((NC * NB <= 384) ? 16 : 8))) { \
         constexpr int kW = (NC * NB <= 384) ? 16 : 8;                       \
         *w = kW;                                                            \
         *threads = rot_sb_block(NC, NB, kW);                                \
@@ -36,15 +43,17 @@ RotFsFn pick_rot_fs(int ndop) {
                               : "k_col_rot_sb<" #NC "," #NB ",8>");         \
     }
 
-RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
+RotSbFn pick_rot_sb(int n_coh, int nb, int want_w, int* w, int* threads) {
     ACQ_RSB_CASE(20, 25) ACQ_RSB_CASE(10, 20) ACQ_RSB_CASE(20, 12) ACQ_RSB_CASE(10, 16) ACQ_RSB_CASE(10, 4)
     ACQ_RSB_CASE(20, 20) ACQ_RSB_CASE(10, 25) ACQ_RSB_CASE(20, 16) ACQ_RSB_CASE(10, 12) ACQ_RSB_CASE(20, 10)
+    ACQ_RSB_W_CASE(20, 25, 4)
     return nullptr;
 }
 
 #define ACQ_SSB_CASE(N1, N2, W, NDB)                                                                 \
-    if (ndop == N1 * N2 && ndb == NDB && (want_w == 0 || want_w == W)) {                              \
+    if (ndop == N1 * N2 && ndb == NDB && (want_w == 0 || want_w == W) && (want_n1 == 0 || want_n1 == N1)) { \
         *w = W;                                                                                      \
+        *n1 = N1;                                                                                    \
         *threads = (1 << (NDB - 1)) * N1 * W;                                                         \
         *smem = sizeof(float2) * ((size_t)(1 + NDB) * N1 * N2 * W + N1 * N2) + 64;                    \
         return named(&k_col_sign_sb<N1, N2, W, NDB>,                                                  \
@@ -53,20 +62,20 @@ RotSbFn pick_rot_sb(int n_coh, int nb, int* w, int* threads) {
 
 // two data bits: the half-spectrum form (same block shape and shared memory as k_col_sign_sb)
 #define ACQ_SFOLD_CASE(N1, N2, W)                                                                    \
-    if (ndop == N1 * N2 && ndb == 2 && (want_w == 0 || want_w == W)) {                                \
+    if (ndop == N1 * N2 && ndb == 2 && (want_w == 0 || want_w == W) && (want_n1 == 0 || want_n1 == N1)) { \
         *w = W;                                                                                      \
+        *n1 = N1;                                                                                    \
         *threads = 2 * N1 * W;                                                                       \
         *smem = sizeof(float2) * ((size_t)3 * N1 * N2 * W + N1 * N2) + 64;                            \
         return named(&k_col_sign_fold<N1, N2, W>, "k_col_sign_fold<" #N1 "," #N2 "," #W ">");        \
     }
 
-SignSbFn pick_sign_sb(int ndop, int ndb, int* w, int* threads, size_t* smem) {
-    // columns per block: the first instantiation listed for the size (ndop 800: four columns, two
-    // CTAs per SM, 5.81 ms vs 6.29 ms with eight on the 40 ms x 2 search), or ACQ_SIGN_W when set
-    const char* e = std::getenv("ACQ_SIGN_W");
-    const int want_w = e ? std::atoi(e) : 0;
-    ACQ_SFOLD_CASE(32, 25, 4) ACQ_SFOLD_CASE(32, 25, 8) ACQ_SFOLD_CASE(32, 20, 8) ACQ_SFOLD_CASE(32, 40, 4)
-    ACQ_SFOLD_CASE(20, 20, 8) ACQ_SFOLD_CASE(20, 10, 16)
+SignSbFn pick_sign_sb(int ndop, int ndb, int want_w, int want_n1, int* w, int* n1, int* threads, size_t* smem) {
+    // the first instantiation listed for a size is its default (ndop 800: 32 x 25, four columns,
+    // two CTAs per SM); the others are the autotuner's alternatives (ACQ_OPT_SEARCH_WIDTH / _SPLIT)
+    ACQ_SFOLD_CASE(32, 25, 4) ACQ_SFOLD_CASE(32, 25, 8) ACQ_SFOLD_CASE(32, 25, 2) ACQ_SFOLD_CASE(40, 20, 2)
+    ACQ_SFOLD_CASE(40, 20, 4) ACQ_SFOLD_CASE(32, 20, 8) ACQ_SFOLD_CASE(32, 40, 4) ACQ_SFOLD_CASE(20, 20, 8)
+    ACQ_SFOLD_CASE(20, 10, 16)
     ACQ_SSB_CASE(16, 25, 8, 1)
     return nullptr;
 }

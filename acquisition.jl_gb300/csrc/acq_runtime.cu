@@ -424,7 +424,7 @@ struct acq_plan {
     // data-bit / bit-edge stage split by sub-blocks
     SignSbFn sign_sb = nullptr;
     size_t smem_ssb = 0;
-    int Wssb = 8, threads_ssb = 256;
+    int Wssb = 8, threads_ssb = 256, n1ssb = 0;
     // rotation stage split by sub-blocks
     RotSbFn rot_sb = nullptr;
     size_t smem_rsb = 0;
@@ -847,6 +847,43 @@ void setup_col_tma(acq_plan* P, int n_prns, int W = 16, int ctas_per_sm = 0) {
     }
 }
 
+// Split bit-edge search (path 1, even ndop): the instantiation for the plan's size with the
+// wanted columns per CTA and first-pass length (0: the size's default). Returns false, leaving
+// the plan's kernel as it was, when none matches.
+bool setup_sign_search(acq_plan* P, int want_w, int want_n1) {
+    const Geometry& g = P->g;
+    if (g.path != 1 || (g.ndop % 2) != 0 || getenv_flag("ACQ_GENERIC_FFT") || (g.n_coh % g.ndb) != 0) return false;
+    int w = 8, n1 = 0, th = 256;
+    size_t smem = 0;
+    SignSbFn fn = pick_sign_sb(g.ndop, g.ndb, want_w, want_n1, &w, &n1, &th, &smem);
+    if (!fn || smem > 220 * 1024) return false;
+    set_smem((const void*)fn, smem);
+    P->sign_sb = fn;
+    P->smem_ssb = smem;
+    P->Wssb = w;
+    P->n1ssb = n1;
+    P->threads_ssb = th;
+    return true;
+}
+
+// Split rotation search (path 2, even ndop), likewise for the columns per CTA.
+bool setup_rot_search(acq_plan* P, int want_w) {
+    const Geometry& g = P->g;
+    if (g.path != 2 || (g.ndop % 2) != 0 || getenv_flag("ACQ_GENERIC_FFT")) return false;
+    int w = 8, th = 256;
+    RotSbFn fn = pick_rot_sb(g.n_coh, g.nb, want_w, &w, &th);
+    if (!fn) return false;
+    const size_t need = sizeof(float2) * ((size_t)2 * g.ndop * w + g.ndop) + sizeof(int) * w +
+                        sizeof(float) * (size_t)g.R * ((size_t)1 << (g.ndb - 1)) * g.n_coh;
+    if (need > 200 * 1024) return false;
+    set_smem((const void*)fn, need);
+    P->rot_sb = fn;
+    P->smem_rsb = need;
+    P->Wrsb = w;
+    P->threads_rsb = th;
+    return true;
+}
+
 void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user_codes) {
     const Geometry& g = P->g;
     CK(cudaSetDevice(P->device));
@@ -919,31 +956,8 @@ void plan_setup(acq_plan* P, const int32_t* prns, int n_prns, const int8_t* user
         if (g.path == 1) P->sign_fs = pick_sign_fs(g.ndop);
         if (g.path == 2) P->rot_fs = pick_rot_fs(g.ndop);
     }
-    if (g.path == 1 && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT") && (g.n_coh % g.ndb) == 0) {
-        int w = 8, th = 256;
-        size_t smem = 0;
-        SignSbFn fn = pick_sign_sb(g.ndop, g.ndb, &w, &th, &smem);
-        if (fn && smem <= 220 * 1024) {
-            set_smem((const void*)fn, smem);
-            P->sign_sb = fn;
-            P->smem_ssb = smem;
-            P->Wssb = w;
-            P->threads_ssb = th;
-        }
-    }
-    if (g.path == 2 && (g.ndop % 2) == 0 && !getenv_flag("ACQ_GENERIC_FFT")) {
-        int w = 8, th = 256;
-        RotSbFn fn = pick_rot_sb(g.n_coh, g.nb, &w, &th);
-        const size_t need = sizeof(float2) * ((size_t)2 * g.ndop * w + g.ndop) + sizeof(int) * w +
-                            sizeof(float) * (size_t)g.R * ((size_t)1 << (g.ndb - 1)) * g.n_coh;
-        if (fn && need <= 200 * 1024) {
-            set_smem((const void*)fn, need);
-            P->rot_sb = fn;
-            P->smem_rsb = need;
-            P->Wrsb = w;
-            P->threads_rsb = th;
-        }
-    }
+    setup_sign_search(P, 0, 0);
+    setup_rot_search(P, 0);
     if (P->sign_fs || P->rot_fs) {
         const size_t per = 2 * 8 + 4 + 2;   // tile + work (float2), stage (float), winner (u16)
         int W = 16;
@@ -2022,6 +2036,8 @@ int acq_plan_get_option(const acq_plan* P, int32_t option, int64_t* value) {
             case ACQ_OPT_TRANSFORM_LENGTH: *value = P->g.fft_tile; break;
             case ACQ_OPT_TILE_MMA: *value = P->tmma ? 1 : 0; break;
             case ACQ_OPT_COLUMN_WAIT_POLLS: *value = P->col_k1 ? P->k1WaitPolls : 0; break;
+            case ACQ_OPT_SEARCH_WIDTH: *value = P->sign_sb ? P->Wssb : P->rot_sb ? P->Wrsb : 0; break;
+            case ACQ_OPT_SEARCH_SPLIT: *value = P->sign_sb ? P->n1ssb : 0; break;
             case ACQ_OPT_COLUMN_WIDTH: *value = P->col_k1 ? P->k1W : P->col_tma ? P->tmaW : 0; break;
             case ACQ_OPT_COLUMN_CTAS_PER_SM: *value = P->col_k1 ? P->k1CtasPerSm : P->col_tma ? P->tmaCtasPerSm : 0; break;
             default: throw AcqError(ACQ_ERR_ARGUMENT, "unknown option " + std::to_string(option));
@@ -2182,6 +2198,26 @@ int acq_plan_set_option(acq_plan* P, int32_t option, int64_t value, int64_t* eff
             setup_col_tma(P, P->n_plan_prns, P->tmaW, P->tmaCtasPerSm);
             setup_tile_mma(P);
             if (effective) *effective = P->tmma ? 1 : 0;
+            return;
+        }
+        if (option == ACQ_OPT_SEARCH_WIDTH || option == ACQ_OPT_SEARCH_SPLIT) {
+            if (value < 1 || value > 1024) throw AcqError(ACQ_ERR_ARGUMENT, "search shape must be in 1:1024");
+            CK(cudaStreamSynchronize(P->stream));
+            const int v = static_cast<int>(value);
+            if (P->sign_sb) {
+                // keep the other dimension where an instantiation has both, else take the value's default
+                if (option == ACQ_OPT_SEARCH_WIDTH) {
+                    if (!setup_sign_search(P, v, P->n1ssb)) setup_sign_search(P, v, 0);
+                } else if (!setup_sign_search(P, P->Wssb, v)) {
+                    setup_sign_search(P, 0, v);
+                }
+                if (effective) *effective = option == ACQ_OPT_SEARCH_WIDTH ? P->Wssb : P->n1ssb;
+            } else if (P->rot_sb && option == ACQ_OPT_SEARCH_WIDTH) {
+                setup_rot_search(P, v);
+                if (effective) *effective = P->Wrsb;
+            } else if (effective) {
+                *effective = 0;
+            }
             return;
         }
         if (option == ACQ_OPT_COLUMN_WAIT_POLLS) {

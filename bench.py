@@ -782,7 +782,7 @@ def main():
         from acqgb300 import autotune as T
         tuned = T.tune(plan, dev, PRNS, reps=3, passes=1, store=False,
                        knobs=("tile_rows", "tile_threads", "tile_blocks", "tile_pad", "column_width",
-                              "column_ctas_per_sm", "tile_mma"))
+                              "column_ctas_per_sm", "tile_mma", "search_width", "search_split"))
 
     # warm-up (device-resident and public API)
     for _ in range(args.warmup):

@@ -199,6 +199,10 @@ int acq_plan_last_kernels(const acq_plan* plan, char* buf, size_t len);
                                         give-up path: one block-wide decision, a full-limit wait for the copies
                                         in flight, ACQ_ERR_TIMEOUT from acq_fetch_results); 0 where the plan
                                         has no such stage */
+#define ACQ_OPT_SEARCH_WIDTH 13      /* bit-edge / rotation search kernel: code-phase columns per CTA (the sizes
+                                        instantiated for the plan's geometry; 0 where it has no such kernel) */
+#define ACQ_OPT_SEARCH_SPLIT 14      /*   bit-edge search: first-pass length N1 of the num_doppler_bins = N1 x N2
+                                        FFT split (instantiated splits; 0 where none) */
 
 /* Set a plan option; ACQ_OPT_FORM selects the kernel form of later acquisitions. The fused
  * form is used only where the plan's sizes have a fused kernel (otherwise plain).

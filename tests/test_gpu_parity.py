@@ -399,7 +399,20 @@ def test_bit_edge_search_workload_geometry():
     res = A.acquire_b(plan, sig, prns, store_power_bins=True)
     ks = plan.last_kernels()
     assert ks.count("k_col_sign_fold<32,25,4>") == 2, ks
-    _compare(res, _oracles("GPSL1CA", 5e6, prns, _complex(sig), **kw), "bit-edge-ndop800")
+    outs = _oracles("GPSL1CA", 5e6, prns, _complex(sig), **kw)
+    _compare(res, outs, "bit-edge-ndop800")
+    # every search shape the autotuner may pick for this size (columns per CTA, FFT split)
+    from acqgb300 import _lib as L
+    for w, n1 in [(8, 32), (2, 32), (2, 40), (4, 40)]:
+        assert plan.set_option(L.ACQ_OPT_SEARCH_SPLIT, n1) == n1
+        assert plan.set_option(L.ACQ_OPT_SEARCH_WIDTH, w) == w
+        assert (plan.get_option(L.ACQ_OPT_SEARCH_WIDTH), plan.get_option(L.ACQ_OPT_SEARCH_SPLIT)) == (w, n1)
+        res = A.acquire_b(plan, sig, prns, store_power_bins=True)
+        kernel = f"k_col_sign_fold<{n1},{800 // n1},{w}>"
+        assert plan.last_kernels().count(kernel) == 2, plan.last_kernels()
+        _compare(res, outs, f"bit-edge-ndop800-{kernel}")
+    # a width the size has no instantiation for keeps the shape in effect
+    assert plan.set_option(L.ACQ_OPT_SEARCH_WIDTH, 3) == 4
 
 
 @pytest.mark.parametrize("n_nc", [1, 2])
@@ -423,6 +436,14 @@ def test_rotation_workload_geometry_all_precisions(n_nc):
         ks = plan.last_kernels()
         assert ks.count(kernel) == n_nc, ks
         _compare(res, outs, f"rotation-l5i-20MHz-n_nc{n_nc}-prec{prec}")
+    # the autotuner's other width for this size
+    from acqgb300 import _lib as L
+    assert plan.set_rotation_precision("fp32") == "fp32"
+    assert plan.set_option(L.ACQ_OPT_SEARCH_WIDTH, 4) == 4
+    assert plan.get_option(L.ACQ_OPT_SEARCH_SPLIT) == 0
+    res = A.acquire_b(plan, sig, prns, store_power_bins=True)
+    assert plan.last_kernels().count("k_col_rot_sb<20,25,4>") == n_nc, plan.last_kernels()
+    _compare(res, outs, f"rotation-l5i-20MHz-n_nc{n_nc}-width4")
 
 
 def test_ragged_batch_recordings_against_the_oracle():
