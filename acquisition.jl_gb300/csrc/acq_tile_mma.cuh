@@ -29,8 +29,11 @@
 namespace acq {
 
 constexpr int kTmmaRows = 128;      // code rows (PRN, block) per CTA: the MMA's M
-constexpr int kTmmaDrainWarps = 8;
+constexpr int kTmmaDrainWarps = 16;
 constexpr int kTmmaThreads = 32 * kTmmaDrainWarps + 32;   // drain warps + the issuing warp
+// code rows one drain warp moves per lag half: the warps of a TMEM lane quarter split the 128
+constexpr int kTmmaDrainRows = 4 * 128 / kTmmaDrainWarps;
+static_assert(kTmmaDrainRows == 32 || kTmmaDrainRows == 64, "32 or 64 code rows per drain warp");
 constexpr int kTmmaStubThreads = 256;
 
 // geometry of the operands for a block size bs <= 256
@@ -331,13 +334,15 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
             }
         }
     } else {
-        // drain warps: warp w reads lags 128 h + 32 (w % 4) + lane and code rows 64 (w / 4) .. + 63;
-        // lane l holds the tile offsets of code rows 64 (w / 4) + l and + 32 + l for the current unit.
+        // drain warps: warp w reads lags 128 h + 32 (w % 4) + lane (its TMEM lane quarter) and code
+        // rows R (w / 4) .. + R - 1, R = kTmmaDrainRows; lane l holds the tile offsets of code rows
+        // R (w / 4) + l (and + 32 + l when R = 64) for the current unit.
         // The next 16 columns' tcgen05.ld is in flight while the current ones are stored; the
         // stores stream (evict-first): the tile is read once, by the Doppler stage, much later.
-        const int sp = warp & 3, cbase = (warp >> 2) * 64;
-        const int64_t my_off = col_off[cbase + lane], my_off2 = col_off[cbase + 32 + lane];
-        const int my_m = col_m[cbase + lane], my_m2 = col_m[cbase + 32 + lane];
+        const int sp = warp & 3, cbase = (warp >> 2) * kTmmaDrainRows;
+        const int64_t my_off = col_off[cbase + lane];
+        const int64_t my_off2 = kTmmaDrainRows == 64 ? col_off[cbase + 32 + lane] : -1;
+        const int my_m = col_m[cbase + lane], my_m2 = kTmmaDrainRows == 64 ? col_m[cbase + 32 + lane] : 0;
         for (int u = 0; u < nu; ++u) {
             const int gu = u0 + u;
             const int step = gu / p.G, rho = gu - (gu / p.G) * p.G;
@@ -364,9 +369,9 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
                 tc_ld8(tb + 128 + 8, im[0] + 8);
                 tc_wait_ld();
 #pragma unroll
-                for (int i = 0; i < 64; i += 16) {
+                for (int i = 0; i < kTmmaDrainRows; i += 16) {
                     const int cb = (i >> 4) & 1;
-                    if (i + 16 < 64) {
+                    if (i + 16 < kTmmaDrainRows) {
                         tc_ld8(tb + i + 16, re[cb ^ 1]);
                         tc_ld8(tb + i + 24, re[cb ^ 1] + 8);
                         tc_ld8(tb + 128 + i + 16, im[cb ^ 1]);
