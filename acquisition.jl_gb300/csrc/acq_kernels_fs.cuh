@@ -953,11 +953,21 @@ __global__ void __launch_bounds__(rot_sb_block(NC, NB, W))
     const int wv = min(W, spc - c0);
     const int n_pat = R * combos;
     const float2* tp = T + static_cast<int64_t>(pi) * ND * spc;
-    for (int w = tid; w < ND * W; w += blockDim.x) {
-        const int e = w / W, t = w - e * W;
-        float2 v = make_float2(0.f, 0.f);
-        if (t < wv) ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 41) v = tp[static_cast<int64_t>(e) * spc + c0 + t];
-        tile[w] = v;
+    {
+        // the block's tile loads in flight together, then the shared-memory stores
+        constexpr int NT = rot_sb_block(NC, NB, W), NL = (ND * W + NT - 1) / NT;
+        float2 tv[NL];
+#pragma unroll
+        for (int u = 0; u < NL; ++u) {
+            const int w = tid + u * NT;
+            const int e = w / W, t = w - e * W;
+            tv[u] = make_float2(0.f, 0.f);
+            if (w < ND * W && t < wv)
+                ACQ_BC(&tp[static_cast<int64_t>(e) * spc + c0 + t], 41) tv[u] = tp[static_cast<int64_t>(e) * spc + c0 + t];
+        }
+#pragma unroll
+        for (int u = 0; u < NL; ++u)
+            if (tid + u * NT < ND * W) tile[tid + u * NT] = tv[u];
     }
     for (int i = tid; i < ND; i += blockDim.x) tws[i] = twD[i];
     if (tid < W) {
