@@ -442,12 +442,17 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
     };
     uint32_t phases = 0u;   // bit b: the parity to wait for on mbar[b]
     if (threadIdx.x == 0 && K > 0) issue(0);
-    for (int k = 0; k < K; ++k) {
+    // step m of work item `item` (kept across iterations: the divisions run once per item)
+    int m = 0, item = blockIdx.x;
+    int grp = 0, cb = 0, k1 = 0, pi = 0;
+    for (int k = 0; k < K; ++k, m = (m + 1 == p.n_nc) ? 0 : m + 1, item += (m == 0) ? gridDim.x : 0) {
         const int b = k & 1;
-        const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
-        const int m = k % p.n_nc;
-        const int grp = item / p.n_cblk, cb = item - grp * p.n_cblk;
-        const int k1 = grp % n1, pi = grp / n1;
+        if (m == 0) {
+            grp = item / p.n_cblk;
+            cb = item - grp * p.n_cblk;
+            k1 = grp % n1;
+            pi = grp / n1;
+        }
         if (m == 0) {   // this item's output rows and per-step offsets (the epilogue synced before)
             for (int i = threadIdx.x; i < (p.n_nc + 1) * N2; i += blockDim.x) {
                 const int mm = i / N2, k2 = i - mm * N2;
