@@ -431,17 +431,17 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
                              ? (n_items - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
                              : 0;
     const int K = my_items * p.n_nc;
-    auto issue = [&](int k) {
-        const int item = blockIdx.x + (k / p.n_nc) * gridDim.x;
-        const int m = k % p.n_nc;
-        const int grp = item / p.n_cblk, cb = item - grp * p.n_cblk;   // grp = pi * n1 + k1
-        const int b = k & 1;
+    // the box of step m of the work item with group grp (= pi * n1 + k1) and column block cb
+    auto issue = [&](int m, int grp, int cb, int b) {
         fence_proxy_async();
         mbar_expect_tx(&mbar[b], tile_bytes);
         tma_load_2d_ef(buf0 + b * BS, &tmap, cb * W, m * p.rows_per_step + grp * N2, &mbar[b]);
     };
     uint32_t phases = 0u;   // bit b: the parity to wait for on mbar[b]
-    if (threadIdx.x == 0 && K > 0) issue(0);
+    if (threadIdx.x == 0 && K > 0) {
+        const int g0 = static_cast<int>(blockIdx.x) / p.n_cblk;
+        issue(0, g0, static_cast<int>(blockIdx.x) - g0 * p.n_cblk, 0);
+    }
     // step m of work item `item` (kept across iterations: the divisions run once per item)
     int m = 0, item = blockIdx.x;
     int grp = 0, cb = 0, k1 = 0, pi = 0;
@@ -469,7 +469,15 @@ __global__ void __launch_bounds__(128) k_col_tma_k1(const __grid_constant__ CUte
             }
             __syncthreads();
         }
-        if (threadIdx.x == 0 && k + 1 < K) issue(k + 1);
+        if (threadIdx.x == 0 && k + 1 < K) {   // the next step's box (a new item: divide once)
+            if (m + 1 < p.n_nc) {
+                issue(m + 1, grp, cb, (k + 1) & 1);
+            } else {
+                const int itn = item + static_cast<int>(gridDim.x);
+                const int gn = itn / p.n_cblk;
+                issue(0, gn, itn - gn * p.n_cblk, (k + 1) & 1);
+            }
+        }
         const bool landed = mbar_wait_bounded(&mbar[b], (phases >> b) & 1u, p.err, 1, p.wait_polls);
         const uint32_t parity_b = (phases >> b) & 1u;
         if (landed) phases ^= 1u << b;

@@ -731,8 +731,10 @@ void setup_col_k1(acq_plan* P, int n_prns, int W, int ctas_per_sm) {
 // one launch per step on the others. The FP32 FFT tiles stay the fallback (and ACQ_GENERIC_FFT
 // keeps the generic kernels).
 bool tile_mma_possible(const acq_plan* P) {
-    return P->tmma_enabled && P->g.bs <= kTmmaMaxBs && !getenv_flag("ACQ_NO_TILE_MMA") &&
-           !getenv_flag("ACQ_GENERIC_FFT");
+    // the drain addresses a step's tile (the plan's PRNs x rows x spc cells) with 32-bit offsets
+    const int64_t step_cells = static_cast<int64_t>(P->n_plan_prns) * P->g.n_coh * P->g.nb * P->g.spc;
+    return P->tmma_enabled && P->g.bs <= kTmmaMaxBs && step_cells < (int64_t{1} << 31) &&
+           !getenv_flag("ACQ_NO_TILE_MMA") && !getenv_flag("ACQ_GENERIC_FFT");
 }
 
 void setup_tile_mma(acq_plan* P) {

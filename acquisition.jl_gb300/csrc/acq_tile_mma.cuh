@@ -350,9 +350,12 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
             if (r < 0) r += p.nb;
             int r2 = my_m2 - rho % p.nb;
             if (r2 < 0) r2 += p.nb;
-            const int64_t rowb = step * p.t_step_stride + static_cast<int64_t>(rho) * p.spc;
-            const int64_t off_l = my_off < 0 ? -1 : rowb + my_off + static_cast<int64_t>(r) * p.bs;
-            const int64_t off_l2 = my_off2 < 0 ? -1 : rowb + my_off2 + static_cast<int64_t>(r2) * p.bs;
+            // cell offsets within the step (the host keeps a step's tile under 2^31 cells), shuffled
+            // as one 32-bit value per code row; the step's base is added once
+            const int64_t sbase = step * p.t_step_stride;
+            const int rowb = rho * p.spc;
+            const int off_l = my_off < 0 ? -1 : rowb + static_cast<int>(my_off) + r * p.bs;
+            const int off_l2 = my_off2 < 0 ? -1 : rowb + static_cast<int>(my_off2) + r2 * p.bs;
             const float isc = p.inv_scale[gu];
             bool ok = true;
             for (int h = 0; h < NH; ++h) {
@@ -360,7 +363,7 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
                 tc_fence_after();
                 const int j = h * 128 + sp * 32 + lane;
                 const bool jok = j < p.bs;
-                float2* base = p.T + j;
+                float2* base = p.T + sbase + j;
                 const uint32_t tb = tmem + (static_cast<uint32_t>(sp * 32) << 16) + h * 256 + cbase;
                 float re[2][16], im[2][16];
                 tc_ld8(tb + 0, re[0]);
@@ -377,10 +380,10 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
                         tc_ld8(tb + 128 + i + 16, im[cb ^ 1]);
                         tc_ld8(tb + 128 + i + 24, im[cb ^ 1] + 8);
                     }
-                    const int64_t ol = i < 32 ? off_l : off_l2;
+                    const int ol = i < 32 ? off_l : off_l2;
 #pragma unroll
                     for (int e = 0; e < 16; ++e) {
-                        const int64_t off = __shfl_sync(0xffffffffu, ol, (i & 31) + e);
+                        const int off = __shfl_sync(0xffffffffu, ol, (i & 31) + e);
                         if (off >= 0 && jok)
                             ACQ_BC(base + off, 6) __stcs(base + off, make_float2(re[cb][e] * isc, im[cb][e] * isc));
                     }
