@@ -30,7 +30,7 @@ namespace acq {
 
 constexpr int kTmmaRows = 128;      // code rows (PRN, block) per CTA: the MMA's M
 constexpr int kTmmaDrainWarps = 16;
-constexpr int kTmmaThreads = 32 * kTmmaDrainWarps + 32;   // drain warps + the issuing warp
+constexpr int kTmmaThreads = 32 * kTmmaDrainWarps + 64;   // drain warps, the issuing warp, the copy warp
 // code rows one drain warp moves per lag half: the warps of a TMEM lane quarter split the 128
 constexpr int kTmmaDrainRows = 4 * 128 / kTmmaDrainWarps;
 static_assert(kTmmaDrainRows == 32 || kTmmaDrainRows == 64, "32 or 64 code rows per drain warp");
@@ -197,8 +197,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // a warp's tcgen05.ld gives 32 consecutive lags of 8 code rows, stored as 256 contiguous bytes
 // per code row. Tensor memory: lag half h of Re D at columns 256 h .. + 127, of Im D at
 // 256 h + 128 .. + 255.
-// Warp roles: warp kTmmaDrainWarps (one elected thread) issues the bulk copies of the Q_s (two
-// buffers) and the MMAs; warps 0 .. kTmmaDrainWarps - 1 move D to the tile. mbarriers:
+// Warp roles: warp kTmmaDrainWarps + 1 (one elected thread) issues the bulk copies of the Q_s (two
+// buffers), warp kTmmaDrainWarps (one elected thread) the MMAs, warps 0 .. kTmmaDrainWarps - 1
+// move D to the tile. mbarriers:
 //   sbar[b]   Q_s of buffer b landed (bulk-copy transaction count)
 //   full[h]   MMAs of lag half h done (tcgen05.commit)
 //   empty[h]  half h drained (one arrival per drain warp)
@@ -269,24 +270,38 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
     const uint32_t tmem = *tslot;
     pdl_wait();   // the operand blocks and their scales (code rows and slots are already in place)
 
-    if (warp == kTmmaDrainWarps) {
+    if (warp == kTmmaDrainWarps + 1) {
+        // copy warp: unit u's operand blocks into buffer u & 1 as soon as the MMAs of unit u - 2
+        // are done with it (one unit ahead of the MMAs)
         if (lane == 0) {
-            // completions asked of each barrier, for the bounded drain on an error
-            uint32_t n_s[2] = {0u, 0u}, n_full[2] = {0u, 0u}, n_free[2] = {0u, 0u};
-            auto prefetch = [&](int u) {
+            uint32_t n_s[2] = {0u, 0u};   // copies issued per buffer, for the bounded drain on an error
+            bool ok = true;
+            for (int u = 0; u < nu; ++u) {
                 const int b = u & 1;
+                if (u >= 2 && !(ok = tmma_wait(&sfree[b], ((u - 2) >> 1) & 1, p.err, abort_flag))) break;
                 ++n_s[b];
 #ifdef ACQ_BOUNDS_CHECK
                 if (!bc_ok(p.stubs + static_cast<int64_t>(u0 + u) * row_bytes, row_bytes, 4)) {
                     mbar_expect_tx(&sbar[b], 0u);   // completes the phase without a copy
-                    return;
+                    continue;
                 }
 #endif
                 mbar_expect_tx(&sbar[b], row_bytes);
                 bulk_load(stub0 + b * row_bytes, p.stubs + static_cast<int64_t>(u0 + u) * row_bytes, row_bytes,
                           &sbar[b]);
-            };
-            for (int u = 0; u < 2 && u < nu; ++u) prefetch(u);
+            }
+            if (!ok) {   // let every copy in flight land before the block's memory is released
+                for (int i = 0; i < 2; ++i)
+                    if (n_s[i]) mbar_wait_bounded(&sbar[i], (n_s[i] - 1) & 1, p.err, 6, 1u << 20);
+            }
+        }
+    } else if (warp == kTmmaDrainWarps) {
+        // issuing thread: per unit, wait for its operand blocks, then per lag half wait until the
+        // drain has emptied that half, issue its MMAs and commit them to full[h]; sfree[b] tells
+        // the copy warp when buffer b may be overwritten
+        if (lane == 0) {
+            // completions asked of each barrier, for the bounded drain on an error
+            uint32_t n_full[2] = {0u, 0u}, n_free[2] = {0u, 0u};
             const uint32_t idesc = tc_idesc_f16(0, 128, kTmmaRows);
             // descriptors differ only in the start-address field (byte address / 16, < 2^14)
             const uint64_t a0 = tc_desc(stub0, 128, 128);
@@ -311,23 +326,14 @@ __global__ void __launch_bounds__(kTmmaThreads, 1) k_tile_mma(TileMmaParams p) {
                     }
                     tc_commit(&full[h]);
                     ++n_full[h];
-                    // with half 0 of unit u queued behind them, the MMAs of unit u - 1 finish; the
-                    // next unit's operand blocks then go into their buffer and have the rest of
-                    // unit u's MMAs to land
-                    if (h == 0 && u >= 1 && u + 1 < nu) {
-                        const int bn = (u + 1) & 1;
-                        if (!(ok = tmma_wait(&sfree[bn], ((u - 1) >> 1) & 1, p.err, abort_flag))) break;
-                        prefetch(u + 1);
-                    }
                 }
                 if (!ok) break;
                 tc_commit(&sfree[b]);
                 ++n_free[b];
             }
             if (!ok) {
-                // let every copy and MMA still in flight land before the block's memory is released
+                // let every MMA still in flight land before the block's memory is released
                 for (int i = 0; i < 2; ++i) {
-                    if (n_s[i]) mbar_wait_bounded(&sbar[i], (n_s[i] - 1) & 1, p.err, 6, 1u << 20);
                     if (n_full[i]) mbar_wait_bounded(&full[i], (n_full[i] - 1) & 1, p.err, 6, 1u << 20);
                     if (n_free[i]) mbar_wait_bounded(&sfree[i], (n_free[i] - 1) & 1, p.err, 6, 1u << 20);
                 }
