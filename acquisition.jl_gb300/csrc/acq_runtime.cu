@@ -1138,8 +1138,8 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
     // +3 % acquisitions/s); on multi-GB tiles the early-resident blocks cost more than the gaps
     // (10 ms x 8 at 5 MHz: -1.3 %)
     const size_t step_tile_bytes = sizeof(float2) * (size_t)g.n_nc * P->prns.size() * g.ndop * g.spc;
-    const bool pdl = use_tmma && P->col_k1 && !P->timing && step_tile_bytes <= (256ull << 20) &&
-                     !getenv_flag("ACQ_NO_PDL");
+    const bool pdl = use_tmma && P->col_k1 && !P->timing &&
+                     (step_tile_bytes <= (256ull << 20) || getenv_flag("ACQ_PDL")) && !getenv_flag("ACQ_NO_PDL");
     if (!use_tmma && !use_tmma_step) {
         t_begin(P, ACQ_KERNEL_FRONTEND);
         klog(P, nullptr, "k_frontend");
