@@ -1179,9 +1179,20 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         const int nprn = static_cast<int>(P->prns.size());
         t_begin(P, ACQ_KERNEL_FRONTEND);
         klog(P, nullptr, "k_tile_stubs");
+        // the column stage's accumulator edges are zeroed by the same launch
+        EdgeZero ez{};
+        if (P->tmaH > 0) {
+            ez.acc = P->accb.as<float>();
+            ez.rows = static_cast<int64_t>(n) * g.ndop;
+            ez.spc = g.spc;
+            ez.spc_eff = g.spc_eff;
+            ez.W = P->col_k1 ? P->k1W : P->tmaW;
+            ez.H = P->tmaH;
+            ez.n_bound = (g.spc + ez.W - 1) / ez.W + 1;
+        }
         k_tile_stubs<<<dim3(G, g.n_nc), kTmmaStubThreads, 0, st>>>(
             d_in, dtype, seg_len, G, g.nb, g.n_coh, g.bs, P->col_pre ? 1 : 0, use_if, if_step, a.d_if_off,
-            P->fftD.tw, P->stubs.as<uint8_t>(), P->invsc.as<float>());
+            P->fftD.tw, P->stubs.as<uint8_t>(), P->invsc.as<float>(), ez);
         t_end(P);
         ++L;
         TileMmaParams tp{};
@@ -1220,7 +1231,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
             t_end(P);
             ++L;
         }
-        if (P->tmaH > 0) {
+        if (P->tmaH > 0 && !use_tmma) {   // (the tensor-core path zeroes them in k_tile_stubs)
             const int wc = P->col_k1 ? P->k1W : P->tmaW;
             const int n_bound = (g.spc + wc - 1) / wc + 1;
             const int64_t rows = static_cast<int64_t>(n) * g.ndop;
@@ -1275,7 +1286,7 @@ int64_t launch_sequence(acq_plan* P, cudaStream_t st, const void* d_in, int dtyp
         klog(P, nullptr, "k_tile_stubs");
         k_tile_stubs<<<dim3(G, g.n_nc), kTmmaStubThreads, 0, st>>>(
             d_in, dtype, seg_len, G, g.nb, g.n_coh, g.bs, 0, use_if, if_step, a.d_if_off, P->fftD.tw,
-            P->stubs.as<uint8_t>(), P->invsc.as<float>());
+            P->stubs.as<uint8_t>(), P->invsc.as<float>(), EdgeZero{});
         t_end(P);
         ++L;
     }

@@ -51,13 +51,22 @@ constexpr int kTmmaMaxSpan = tmma_span(kTmmaMaxBs);
 //   pre = 1: row k + nb k1 = W_ndop^{k k1} sum_q W_{n_coh}^{q k1} u_{k + nb q}   (k1 < n_coh)
 //   pre = 0: row g = u_g
 // u_g[t] = input[(g bs + t) mod seg_len] for t < 2 bs (IF wiped off as k_frontend), 0 beyond.
+// The accumulator cells the Doppler-group column stage adds into atomically (H columns on each
+// side of every column-block boundary), zeroed by this kernel's threads after the operand blocks
+// when acc is set (the column stage runs after the tile, which runs after this kernel).
+struct EdgeZero {
+    float* acc;
+    int64_t rows;
+    int spc, spc_eff, W, H, n_bound;
+};
+
 __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __restrict__ in, int dtype,
                                                                  int64_t seg_len, int G, int nb, int n_coh, int bs,
                                                                  int pre, int use_if, float if_step,
                                                                  const float* __restrict__ if_offset,
                                                                  const float2* __restrict__ twD,
                                                                  uint8_t* __restrict__ stubs,
-                                                                 float* __restrict__ inv_scale) {
+                                                                 float* __restrict__ inv_scale, EdgeZero ez) {
     __shared__ __align__(16) uint16_t xh[4][kTmmaMaxSpan];
     __shared__ float red[kTmmaStubThreads / 32];
     pdl_trigger();
@@ -148,6 +157,22 @@ __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __r
         w.z = static_cast<uint32_t>(src[4]) | (static_cast<uint32_t>(src[5]) << 16);
         w.w = static_cast<uint32_t>(src[6]) | (static_cast<uint32_t>(src[7]) << 16);
         ACQ_BC(&out[idx], 2) out[idx] = w;
+    }
+    if (ez.acc) {
+        const int per_row = ez.n_bound * 2 * ez.H;
+        const int64_t total = ez.rows * per_row;
+        const int64_t nthr = static_cast<int64_t>(gridDim.x) * gridDim.y * blockDim.x;
+        for (int64_t q = (static_cast<int64_t>(blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x + tid; q < total;
+             q += nthr) {
+            const int64_t r = q / per_row;
+            const int e = static_cast<int>(q - r * per_row);
+            const int jb = e / (2 * ez.H), o = e - jb * 2 * ez.H - ez.H;   // boundary jb, offset in [-H, H)
+            const int b0 = jb == ez.n_bound - 1 ? ez.spc : jb * ez.W;
+            int c = b0 + o;
+            if (c < 0) c += ez.spc;
+            if (c >= ez.spc) c -= ez.spc;
+            ACQ_BC(&ez.acc[r * ez.spc_eff + c], 23) ez.acc[r * ez.spc_eff + c] = 0.f;
+        }
     }
 }
 

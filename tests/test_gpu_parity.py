@@ -373,7 +373,8 @@ def test_headline_workload_exact_input_and_tuned_shapes():
     assert plan.set_option(L.ACQ_OPT_COLUMN_WIDTH, 128) == 128
     assert plan.set_option(L.ACQ_OPT_COLUMN_CTAS_PER_SM, 4) == 4
     res = A.acquire_b(plan, sig, prns, store_power_bins=True)
-    assert plan.last_kernels() == ["k_tile_stubs", "k_tile_mma", "k_zero_edges", "k_col_tma_k1<20>", "k_edge_peaks",
+    # (the accumulator's block-boundary edges are zeroed inside k_tile_stubs)
+    assert plan.last_kernels() == ["k_tile_stubs", "k_tile_mma", "k_col_tma_k1<20>", "k_edge_peaks",
                                    "k_extract"], plan.last_kernels()
     outs = _oracles("GPSL1CA", 5e6, prns, _complex(sig), **kw)
     _compare(res, outs, "headline-32prn")
