@@ -162,9 +162,10 @@ __global__ void __launch_bounds__(kTmmaStubThreads) k_tile_stubs(const void* __r
         const int per_row = ez.n_bound * 2 * ez.H;
         const int64_t total = ez.rows * per_row;
         const int64_t nthr = static_cast<int64_t>(gridDim.x) * gridDim.y * blockDim.x;
+        const bool narrow = total < (int64_t{1} << 31);   // 32-bit index arithmetic
         for (int64_t q = (static_cast<int64_t>(blockIdx.y) * gridDim.x + blockIdx.x) * blockDim.x + tid; q < total;
              q += nthr) {
-            const int64_t r = q / per_row;
+            const int64_t r = narrow ? static_cast<int>(q) / per_row : q / per_row;
             const int e = static_cast<int>(q - r * per_row);
             const int jb = e / (2 * ez.H), o = e - jb * 2 * ez.H - ez.H;   // boundary jb, offset in [-H, H)
             const int b0 = jb == ez.n_bound - 1 ? ez.spc : jb * ez.W;
