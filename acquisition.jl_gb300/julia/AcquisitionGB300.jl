@@ -158,7 +158,8 @@ end
 # ---- plan options (ACQ_OPT_* of include/acqgb300.h: launch shapes, kernel form, precision) ----
 const OPTIONS = Dict(:form => 0, :rotation_precision => 1, :mma_scale_log2 => 2, :tile_threads => 3,
                      :tile_blocks => 4, :tile_pad => 5, :column_width => 6, :column_ctas_per_sm => 7,
-                     :doppler_precision => 8, :tile_rows => 9, :transform_length => 10, :tile_mma => 11)
+                     :doppler_precision => 8, :tile_rows => 9, :transform_length => 10, :tile_mma => 11,
+                     :column_wait_polls => 12, :search_width => 13, :search_split => 14)
 
 "Set a plan option; returns the value in effect (launch shapes change results only within FP32 rounding)."
 function set_option!(plan::AcquisitionPlan, opt::Symbol, value::Integer)

@@ -43,6 +43,16 @@ def test_python_option_constants_match_the_header():
             assert getattr(L, name) == int(val), name
 
 
+def test_julia_option_table_matches_the_header():
+    header = open(os.path.join(ROOT, "include", "acqgb300.h")).read()
+    opts = {name: int(v) for name, v in re.findall(r"#define ACQ_OPT_(\w+)\s+(-?\d+)", header)}
+    jl = open(os.path.join(ROOT, "acquisition.jl_gb300", "julia", "AcquisitionGB300.jl")).read()
+    table = jl[jl.index("const OPTIONS = Dict("):]
+    table = table[:table.index(")\n")]
+    got = {name.upper(): int(v) for name, v in re.findall(r":(\w+) => (\d+)", table)}
+    assert got == opts, set(got.items()) ^ set(opts.items())
+
+
 def test_result_struct_layout():
     assert C.sizeof(L.Result) == 72
     assert C.sizeof(L.PlanDesc) == 56
