@@ -1867,9 +1867,28 @@ int acq_acquire(acq_plan* P, const void* samples, int32_t dtype, int64_t n_sampl
         const int64_t need = static_cast<int64_t>(g.n_nc) * g.n_coh * g.spc;
         const int64_t ncopy = std::min<int64_t>(n_samples, need);
         CK(cudaSetDevice(P->device));
-        P->input.ensure(eb * std::max<int64_t>(ncopy, 1));
-        CK(cudaMemcpyAsync(P->input.p, samples, eb * ncopy, cudaMemcpyHostToDevice, P->stream));
-        enqueue_acquire(P, P->input.p, dtype, n_samples, prns, n_prns, interm_freq_hz, flags);
+        // The tensor-core all-steps path reads a small (<= 256 KB) page-locked, device-mapped
+        // caller buffer in place: its operand-block kernel reads the samples across the host link
+        // itself, which saves the copy's fixed cost (1 ms at 4 MHz: e2e +2-4 %). Larger inputs copy
+        // first (10 ms x 8 at 5 MHz, 1.6 MB: the in-place reads made the call 16 % slower: each
+        // sample is read several times), as do other paths and pageable buffers.
+        // (ACQ_NO_ZERO_COPY=1: always copy.)
+        const void* d_in = nullptr;
+        const bool tensor_path = P->tmma && P->col_tma && !P->dft_mma && !(P->fused && P->form == ACQ_FORM_FUSED);
+        if (tensor_path && eb * ncopy <= (256u << 10) && !getenv_flag("ACQ_NO_ZERO_COPY")) {
+            cudaPointerAttributes pa{};
+            if (cudaPointerGetAttributes(&pa, samples) == cudaSuccess) {
+                if (pa.type == cudaMemoryTypeHost && pa.devicePointer) d_in = pa.devicePointer;
+            } else {
+                cudaGetLastError();
+            }
+        }
+        if (!d_in) {
+            P->input.ensure(eb * std::max<int64_t>(ncopy, 1));
+            CK(cudaMemcpyAsync(P->input.p, samples, eb * ncopy, cudaMemcpyHostToDevice, P->stream));
+            d_in = P->input.p;
+        }
+        enqueue_acquire(P, d_in, dtype, n_samples, prns, n_prns, interm_freq_hz, flags);
         fetch(P, results, power_bins);
     });
 }
