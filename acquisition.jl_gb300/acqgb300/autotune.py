@@ -84,6 +84,15 @@ def apply(plan, settings: dict) -> dict:
     return eff
 
 
+def unavailable(settings: dict, eff: dict) -> bool:
+    """True when a shape cannot be timed as asked: an option failed, or a requested value has no
+    instantiation for the plan's sizes (the option kept another and reads it back)."""
+    if any(v is None for v in eff.values()):
+        return True
+    return any(k in KNOBS and k not in ZERO_IS_A_VALUE and settings[k] and eff.get(k) != settings[k]
+               for k in settings)
+
+
 def plan_key(plan, dtype_name: str) -> str:
     import torch
     g = plan.geometry
@@ -165,12 +174,7 @@ def tune(plan, signal_dev, prns, *, reps: int = 3, passes: int = 2, cache: str |
     stream = torch.cuda.ExternalStream(plan.stream_handle(), device=signal_dev.device)
 
     def cost(settings):
-        eff = apply(plan, settings)
-        if any(v is None for v in eff.values()):
-            return float("inf")
-        # a value the plan's sizes have no instantiation for (the option kept another)
-        if any(k in KNOBS and k not in ZERO_IS_A_VALUE and settings[k] and eff.get(k) != settings[k]
-               for k in settings):
+        if unavailable(settings, apply(plan, settings)):
             return float("inf")
         acquire_device(plan, signal_dev, prns)   # warm-up (and smem limits)
         ts = []

@@ -64,3 +64,47 @@ def test_tile_mma_is_a_candidate_knob():
 
     cands = T.candidates(P())
     assert cands["tile_mma"] == [1, 0]
+
+
+class _KeepingPlan(_FakePlan):
+    """Search widths other than 4 and 8 have no instantiation: the option keeps the old value."""
+
+    def __init__(self):
+        super().__init__()
+        self.width = 4
+
+    def set_option(self, opt, value):
+        self.calls.append((opt, value))
+        if opt == T.KNOBS["search_width"]:
+            if value in (4, 8):
+                self.width = value
+            return self.width
+        return value
+
+
+def test_shapes_without_an_instantiation_are_skipped():
+    plan = _KeepingPlan()
+    ok = {"search_width": 8, "column_width": 64}
+    assert not T.unavailable(ok, T.apply(plan, ok))
+    missing = {"search_width": 2, "column_width": 64}
+    assert T.unavailable(missing, T.apply(plan, missing))
+    assert T.unavailable({"tile_threads": 64}, {"tile_threads": None})
+    # tile_mma = 0 is a setting, read back as 0
+    assert not T.unavailable({"tile_mma": 0}, T.apply(plan, {"tile_mma": 0}))
+    # coordinate descent never keeps an unavailable shape
+    def cost(sh):
+        return float("inf") if T.unavailable(sh, T.apply(plan, sh)) else {4: 2.0, 8: 1.5}[sh["search_width"]]
+    best, c, _ = T.coordinate_descent(cost, {"search_width": 4}, {"search_width": [2, 4, 8, 16]})
+    assert best == {"search_width": 8} and c == 1.5
+
+
+def test_search_knobs_are_candidates():
+    class G:
+        num_blocks = 20
+        num_coherently_integrated_code_periods = 40
+
+    class P:
+        geometry = G()
+
+    cands = T.candidates(P())
+    assert set(cands["search_width"]) >= {2, 4, 8} and set(cands["search_split"]) >= {25, 32, 40}
