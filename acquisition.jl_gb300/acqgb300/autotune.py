@@ -57,7 +57,8 @@ def candidates(plan) -> dict:
     blocks = sorted({b for b in (1, 2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 25) if b <= nb})
     rows = [1, 2] if plan.geometry.num_coherently_integrated_code_periods >= 2 else [1]
     return {"tile_rows": rows, "tile_threads": [64, 128, 192, 256], "tile_blocks": blocks, "tile_pad": [0, 1, 9],
-            "column_width": [8, 12, 16, 20, 24, 32, 64, 128, 256], "column_ctas_per_sm": [1, 2, 3, 4, 6], "form": ["plain", "fused"],
+            "column_width": [8, 12, 16, 20, 24, 32, 48, 64, 96, 128, 192, 256], "column_ctas_per_sm": [1, 2, 3, 4, 5, 6],
+            "form": ["plain", "fused"],
             "tile_mma": [1, 0], "search_width": [2, 4, 8, 16], "search_split": [20, 25, 32, 40]}
 
 
