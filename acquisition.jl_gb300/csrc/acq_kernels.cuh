@@ -37,6 +37,67 @@ __device__ __forceinline__ float2 load_sample(const void* p, int dtype, int64_t 
     }
 }
 
+// ------------------------------------------------------------------ input upload
+// Recordings in page-locked, device-mapped host memory (cudaHostAlloc, cudaHostRegister, pinned
+// torch tensors) reach the device through this gather: every SM issues 16-byte loads across the
+// host link, each byte is read once, and one launch moves up to kCopySegs recordings. Segment s
+// copies vec[s + 1] - vec[s] 16-byte vectors, then tail[s] (< 16) bytes, from src[s] to dst[s];
+// both addresses are 16-byte aligned. Vector i of the flattened list lies in the segment whose
+// range holds it (binary search over the prefix in shared memory).
+constexpr int kCopySegs = 64;
+constexpr int kCopyThreads = 256;
+constexpr int kCopyUnroll = 4;      // loads in flight per thread
+struct CopyList {
+    const unsigned char* src[kCopySegs];
+    unsigned char* dst[kCopySegs];
+    int64_t vec[kCopySegs + 1];     // prefix of 16-byte vectors
+    int tail[kCopySegs];
+    int n;
+};
+
+__global__ void __launch_bounds__(kCopyThreads) k_copy_in(CopyList L) {
+    __shared__ int64_t pre[kCopySegs + 1];
+    const int tid = threadIdx.x;
+    const int n = L.n;
+    for (int s = tid; s <= n; s += kCopyThreads) pre[s] = L.vec[s];
+    __syncthreads();
+    const int64_t total = pre[n];
+    constexpr int kChunk = kCopyThreads * kCopyUnroll;
+    for (int64_t c = static_cast<int64_t>(blockIdx.x) * kChunk; c < total; c += static_cast<int64_t>(gridDim.x) * kChunk) {
+        uint4 v[kCopyUnroll];
+        int seg[kCopyUnroll];
+        int64_t off[kCopyUnroll];
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u) {
+            const int64_t i = c + u * kCopyThreads + tid;
+            seg[u] = -1;
+            if (i < total) {
+                int lo = 0, hi = n - 1;   // the last s with pre[s] <= i
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (pre[mid] <= i) lo = mid;
+                    else hi = mid - 1;
+                }
+                seg[u] = lo;
+                off[u] = i - pre[lo];
+                v[u] = reinterpret_cast<const uint4*>(L.src[lo])[off[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kCopyUnroll; ++u)
+            if (seg[u] >= 0) {
+                uint4* d = reinterpret_cast<uint4*>(L.dst[seg[u]]) + off[u];
+                ACQ_BC(d, 24) *d = v[u];
+            }
+    }
+    if (blockIdx.x == 0)
+        for (int s = 0; s < n; ++s)
+            if (tid < L.tail[s]) {
+                const int64_t b = (pre[s + 1] - pre[s]) * 16 + tid;
+                ACQ_BC(L.dst[s] + b, 25) L.dst[s][b] = L.src[s][b];
+            }
+}
+
 // ------------------------------------------------------------------ (a) front end
 // Downconversion (src/acquire.jl:92-104) fused with the double-block FFT of every
 // wrapped double block (src/coherent_integration.jl:12-56). One CTA per (step, block).

@@ -1852,6 +1852,59 @@ bool empty_request(acq_plan* P, int64_t n_samples, int32_t n_prns, uint32_t flag
     return true;
 }
 
+namespace {
+// Device address of a page-locked, device-mapped host buffer; null for pageable or device memory
+// and with ACQ_NO_ZERO_COPY=1 (every upload then goes through the copy engines).
+const void* mapped_host(const void* h) {
+    if (getenv_flag("ACQ_NO_ZERO_COPY")) return nullptr;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
+struct Upload {
+    const void* host;     // caller's buffer
+    const void* mapped;   // its device address (mapped_host), or null
+    void* dst;            // device destination
+    size_t bytes;
+};
+
+// Host -> device copies of recordings. Mapped buffers whose addresses are 16-byte aligned go
+// through k_copy_in (one launch per kCopySegs of them: at 1.6 MB and up, the SMs' loads across the
+// host link outrun a copy-engine transfer), the others through cudaMemcpyAsync. Enqueued on st.
+void upload_inputs(const std::vector<Upload>& ups, int device, cudaStream_t st) {
+    CopyList L{};
+    int sms = 0;
+    auto flush = [&] {
+        if (!L.n) return;
+        if (!sms) CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const int64_t chunk = static_cast<int64_t>(kCopyThreads) * kCopyUnroll;
+        const int64_t blocks = (L.vec[L.n] + chunk - 1) / chunk;
+        const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(blocks, 8ll * sms)));
+        k_copy_in<<<grid, kCopyThreads, 0, st>>>(L);
+        CK(cudaGetLastError());
+        L = CopyList{};
+    };
+    for (const Upload& u : ups) {
+        if (!u.bytes) continue;
+        const bool aligned = ((reinterpret_cast<uintptr_t>(u.mapped) | reinterpret_cast<uintptr_t>(u.dst)) & 15) == 0;
+        if (u.mapped && aligned) {
+            L.src[L.n] = static_cast<const unsigned char*>(u.mapped);
+            L.dst[L.n] = static_cast<unsigned char*>(u.dst);
+            L.tail[L.n] = static_cast<int>(u.bytes & 15);
+            L.vec[L.n + 1] = L.vec[L.n] + static_cast<int64_t>(u.bytes >> 4);
+            if (++L.n == kCopySegs) flush();
+        } else {
+            CK(cudaMemcpyAsync(u.dst, u.host, u.bytes, cudaMemcpyHostToDevice, st));
+        }
+    }
+    flush();
+}
+}  // namespace
+
 int acq_acquire(acq_plan* P, const void* samples, int32_t dtype, int64_t n_samples, const int32_t* prns,
                 int32_t n_prns, double interm_freq_hz, uint32_t flags, acq_result* results, float* power_bins) {
     return guarded([&] {
@@ -1869,23 +1922,17 @@ int acq_acquire(acq_plan* P, const void* samples, int32_t dtype, int64_t n_sampl
         CK(cudaSetDevice(P->device));
         // The tensor-core all-steps path reads a small (<= 256 KB) page-locked, device-mapped
         // caller buffer in place: its operand-block kernel reads the samples across the host link
-        // itself, which saves the copy's fixed cost (1 ms at 4 MHz: e2e +2-4 %). Larger inputs copy
-        // first (10 ms x 8 at 5 MHz, 1.6 MB: the in-place reads made the call 16 % slower: each
-        // sample is read several times), as do other paths and pageable buffers.
-        // (ACQ_NO_ZERO_COPY=1: always copy.)
-        const void* d_in = nullptr;
+        // itself, which saves the copy's fixed cost (1 ms at 4 MHz: e2e +2-4 %). Larger inputs are
+        // uploaded first (10 ms x 8 at 5 MHz, 1.6 MB: the in-place reads made the call 16 % slower:
+        // each sample is read several times), as are inputs of other paths: mapped buffers by the
+        // k_copy_in gather, pageable ones by the copy engines. (ACQ_NO_ZERO_COPY=1: always the
+        // copy engines.)
+        const void* mapped = mapped_host(samples);
         const bool tensor_path = P->tmma && P->col_tma && !P->dft_mma && !(P->fused && P->form == ACQ_FORM_FUSED);
-        if (tensor_path && eb * ncopy <= (256u << 10) && !getenv_flag("ACQ_NO_ZERO_COPY")) {
-            cudaPointerAttributes pa{};
-            if (cudaPointerGetAttributes(&pa, samples) == cudaSuccess) {
-                if (pa.type == cudaMemoryTypeHost && pa.devicePointer) d_in = pa.devicePointer;
-            } else {
-                cudaGetLastError();
-            }
-        }
+        const void* d_in = tensor_path && eb * ncopy <= (256u << 10) ? mapped : nullptr;
         if (!d_in) {
             P->input.ensure(eb * std::max<int64_t>(ncopy, 1));
-            CK(cudaMemcpyAsync(P->input.p, samples, eb * ncopy, cudaMemcpyHostToDevice, P->stream));
+            upload_inputs({{samples, mapped, P->input.p, eb * static_cast<size_t>(ncopy)}}, P->device, P->stream);
             d_in = P->input.p;
         }
         enqueue_acquire(P, d_in, dtype, n_samples, prns, n_prns, interm_freq_hz, flags);
@@ -1970,11 +2017,13 @@ int acq_batch_upload(acq_batch* B, const void* const* host) {
     return guarded([&] {
         if (!B || !host) throw AcqError(ACQ_ERR_ARGUMENT, "null argument");
         CK(cudaSetDevice(B->device));
+        std::vector<Upload> ups(B->items.size());
         for (size_t i = 0; i < B->items.size(); ++i) {
             if (!host[i]) throw AcqError(ACQ_ERR_ARGUMENT, "null recording for batch item " + std::to_string(i));
-            CK(cudaMemcpyAsync(B->arena.as<unsigned char>() + B->items[i].in_off, host[i], B->items[i].in_bytes,
-                               cudaMemcpyHostToDevice, B->s0));
+            ups[i] = {host[i], mapped_host(host[i]), B->arena.as<unsigned char>() + B->items[i].in_off,
+                      B->items[i].in_bytes};
         }
+        upload_inputs(ups, B->device, B->s0);
     });
 }
 

@@ -29,6 +29,24 @@ def test_ragged_batch_matches_single_acquisitions():
     bt.close()
 
 
+def test_batch_upload_from_pinned_memory():
+    # page-locked recordings go through the k_copy_in gather, one launch for every item; the
+    # results equal those of the same recordings in pageable memory (copy engines)
+    import torch
+    recs = synth.ragged_batch(seed=13, n_recordings=6, max_nnc=2)
+    cache = B.PlanCache()
+    bt = B.AcquisitionBatch(B.batch_from_recordings(recs, cache))
+    ref = bt.run([np.array(r["samples"]) for r in recs])
+    pinned = [torch.from_numpy(np.ascontiguousarray(r["samples"])).pin_memory() for r in recs]
+    for rep in range(2):
+        got = bt.run([p.numpy() for p in pinned])
+        for res, rr in zip(got, ref):
+            for a, b in zip(res, rr):
+                assert (a.peak_doppler_bin, a.peak_code_bin, a.noise_power) == (b.peak_doppler_bin, b.peak_code_bin,
+                                                                               b.noise_power)
+    bt.close()
+
+
 def test_batch_detects_planted_satellites():
     recs = synth.ragged_batch(seed=5, n_recordings=6, max_nnc=4)
     cache = B.PlanCache()

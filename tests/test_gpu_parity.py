@@ -156,6 +156,34 @@ def test_pinned_host_input_read_in_place(n_coh, n_nc):
         assert [(a.peak_doppler_bin, a.peak_code_bin) for a in again] == [(a.peak_doppler_bin, a.peak_code_bin) for a in ref]
 
 
+@pytest.mark.parametrize("fs,n_coh,n_nc,kind,offset,tile_mma", [
+    (5e6, 10, 2, "ci16", 0, 1),      # 400 KB on the tensor-core path: the k_copy_in gather
+    (4e6, 1, 2, "cf32", 0, 0),       # FFT tile: gathered at any size
+    (1.023e6, 1, 3, "ci8", 0, 0),    # 6138 bytes: 383 16-byte vectors and a 10-byte tail
+    (4e6, 1, 2, "cf32", 1, 0),       # one sample in: 8-byte aligned, so the copy engines
+])
+def test_pinned_host_input_uploaded(fs, n_coh, n_nc, kind, offset, tile_mma):
+    # page-locked recordings that are not read in place are uploaded by the gather kernel (by the
+    # copy engines when not 16-byte aligned); the results equal those from pageable memory
+    import torch
+    from acqgb300 import _lib as L
+    a_sys = A.GPSL1CA()
+    prns = [7, 30]
+    plan = A.plan_acquire(a_sys, fs, prns, num_coherently_integrated_code_periods=n_coh,
+                          num_noncoherent_accumulations=n_nc)
+    assert plan.set_option(L.ACQ_OPT_TILE_MMA, tile_mma) == tile_mma
+    n = n_nc * n_coh * plan.samples_per_code + offset
+    x = synth.synth(a_sys, fs, n, [synth.Satellite(7, 45.0, -2300.0, 312.4)], 31).astype(np.complex64)
+    x = {"cf32": x, "ci16": synth.to_ci16(x), "ci8": synth.to_ci8_3bit(x)}[kind]
+    pinned = torch.from_numpy(x).pin_memory()
+    host = pinned.numpy()[offset:]
+    got = A.acquire_b(plan, host, prns, store_power_bins=True)
+    ref = A.acquire_b(plan, np.array(host), prns, store_power_bins=True)
+    for g, r in zip(got, ref):
+        assert (g.peak_doppler_bin, g.peak_code_bin, g.noise_power) == (r.peak_doppler_bin, r.peak_code_bin, r.noise_power)
+        assert np.array_equal(np.asarray(g.power_bins), np.asarray(r.power_bins))
+
+
 def test_fused_and_plain_forms_agree():
     sats = [synth.Satellite(7, 41.0, -3300.0, 612.4)]
     a_sys = A.GPSL1CA()
