@@ -146,6 +146,28 @@ def test_cfar_threshold_matches_scipy(M):
     assert A.cfar_threshold(0.01, 1) == pytest.approx(-math.log(0.01), rel=1e-12)
 
 
+@pytest.mark.parametrize("system,fs,n_coh,rotations", [("GPSL5I", 12e6, 10, 10), ("GPSL1CA", 2.048e6, 1, 1)])
+def test_num_cells_count_the_rotation_expansion(system, fs, n_coh, rotations):
+    # src/Acquisition.jl:124-142 (issue #70, test/secondary_code_search.jl:473-530): on the rotation
+    # path the peak is taken over num_secondary_rotations times the Doppler x code-phase cells,
+    # get_num_cells counts them, and is_detected flips exactly at the threshold for that count;
+    # off the rotation path the count is the bare grid
+    from types import SimpleNamespace
+    plan = O.plan_acquire(SYS[system][1], fs, [1], num_coherently_integrated_code_periods=n_coh, precision="f32")
+    assert plan.num_secondary_rotations == rotations
+    ndop, spc = plan.num_doppler_bins, plan.num_blocks * plan.block_size
+    r = SimpleNamespace(dopplers=np.zeros(ndop), num_blocks=plan.num_blocks, block_size=plan.block_size,
+                        num_secondary_rotations=plan.num_secondary_rotations, num_noncoherent_integrations=1,
+                        peak_to_noise_ratio=0.0)
+    assert A.get_num_cells(r) == rotations * ndop * spc
+    thr = A.cfar_threshold(0.01, A.get_num_cells(r), num_noncoherent_integrations=1)
+    assert thr > A.cfar_threshold(0.01, ndop * spc) or rotations == 1
+    r.peak_to_noise_ratio = np.float32(thr * (1 + 1e-6))
+    assert A.is_detected(r, pfa=0.01)
+    r.peak_to_noise_ratio = np.float32(thr * (1 - 1e-6))
+    assert not A.is_detected(r, pfa=0.01)
+
+
 def test_cfar_argument_errors():
     for bad in [(0.0, 100), (1.0, 100), (-0.1, 100), (0.01, 0)]:
         with pytest.raises(A.ArgumentError):
