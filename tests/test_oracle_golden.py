@@ -339,3 +339,34 @@ def test_fp32_oracle_against_fp64_oracle():
         rel = np.abs(sa.power - sb.power).max() / sb.power.max()
         assert rel < 1e-5
         assert (a.peak_doppler_bin, a.peak_code_bin) == (b.peak_doppler_bin, b.peak_code_bin)
+
+
+def test_cn0_is_per_hz_independent_of_coherent_length():
+    # test/acquire.jl:462-520: C/N0 divides the coherent time back out, so the estimate does not
+    # climb with num_coherently_integrated_code_periods (mean over 8 code phases, detected trials)
+    fs, true_cn0 = 4e6, 45
+    reported = []
+    for n in (1, 2, 4, 5, 10):
+        plan = O.plan_acquire(G.GPSL1CA, fs, [1], num_coherently_integrated_code_periods=n,
+                              min_doppler_coverage=25_000.0)
+        est = []
+        for k in range(1, 9):
+            sig = _test_signal(G.GPSL1CA, 1, 4000 * n + 100, fs, 1234.0, (k - 0.5) * 1023 / 8 + 0.137, true_cn0,
+                               700 + k)
+            r = O.acquire_b(plan, sig, [1], subsample_interpolation=True)[0]
+            if O.is_detected(r):
+                est.append(r.CN0)
+        assert len(est) >= 5, n
+        reported.append(sum(est) / len(est))
+    assert all(abs(c - true_cn0) <= 6.0 for c in reported), reported
+    assert max(reported) - min(reported) < 4.0, reported
+    assert reported[-1] - reported[0] < 2.0, reported
+
+
+def test_peak_to_noise_ratio_consistent_with_cn0():
+    # test/cfar.jl:117-133: a stronger signal has both the larger PNR and the larger C/N0
+    plan = O.plan_acquire(G.GPSL1CA, 2.048e6, [1])
+    strong = O.acquire_b(plan, _test_signal(G.GPSL1CA, 1, 2048, 2.048e6, 1000.0, 200.0, 55, 11), [1])[0]
+    weak = O.acquire_b(plan, _test_signal(G.GPSL1CA, 1, 2048, 2.048e6, 1000.0, 200.0, 35, 11), [1])[0]
+    assert strong.peak_to_noise_ratio > weak.peak_to_noise_ratio
+    assert strong.CN0 > weak.CN0
