@@ -370,3 +370,23 @@ def test_peak_to_noise_ratio_consistent_with_cn0():
     weak = O.acquire_b(plan, _test_signal(G.GPSL1CA, 1, 2048, 2.048e6, 1000.0, 200.0, 35, 11), [1])[0]
     assert strong.peak_to_noise_ratio > weak.peak_to_noise_ratio
     assert strong.CN0 > weak.CN0
+
+
+@pytest.mark.parametrize("n_coh,flipped", [(40, [(20, 40)]), (60, [(20, 40)])])
+def test_bit_transitions_at_zero_doppler_keep_the_peak(n_coh, flipped):
+    # test/noncoherent_integration.jl:602-701: data bits +1 -1 (40 ms) and +1 -1 +1 (60 ms) at 0 Hz;
+    # the data-bit search recovers the peak of the same signal without transitions (rtol 0.1) and
+    # the pattern it picks flips the second bit against the first
+    fs = 2.048e6
+    clean = _test_signal(G.GPSL1CA, 1, n_coh * 2048, fs, 0.0, 0.0, 60, 42)
+    sig = clean.copy()
+    for a, b in flipped:
+        sig[a * 2048:b * 2048] *= -1
+    plan = O.plan_acquire(G.GPSL1CA, fs, [1], min_doppler_coverage=10_000.0,
+                          num_coherently_integrated_code_periods=n_coh)
+    assert plan.num_data_bits == n_coh // 20
+    ref = O.acquire_b(plan, clean, [1])[0]
+    got = O.acquire_b(plan, sig, [1])[0]
+    assert got.peak_power == pytest.approx(ref.peak_power, rel=0.1)
+    assert (got.peak_doppler_bin, got.peak_code_bin) == (ref.peak_doppler_bin, ref.peak_code_bin)
+    assert ref.sign_pattern == 0 and got.sign_pattern != 0
