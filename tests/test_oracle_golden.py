@@ -390,3 +390,37 @@ def test_bit_transitions_at_zero_doppler_keep_the_peak(n_coh, flipped):
     assert got.peak_power == pytest.approx(ref.peak_power, rel=0.1)
     assert (got.peak_doppler_bin, got.peak_code_bin) == (ref.peak_doppler_bin, ref.peak_code_bin)
     assert ref.sign_pattern == 0 and got.sign_pattern != 0
+
+
+def test_multistep_two_prns_planted_and_absent():
+    # test/acquire.jl:137-156: the multistep path over two PRNs finds the planted one and not the other
+    fs = 2.048e6
+    plan = O.plan_acquire(G.GPSL1CA, fs, [1, 2], num_noncoherent_accumulations=2)
+    sig = _test_signal(G.GPSL1CA, 1, 2 * 2048, fs, 800.0, 150.0, 45, 13).astype(np.complex64)
+    r1, r2 = O.acquire_b(plan, sig, [1, 2])
+    assert O.is_detected(r1) and abs(r1.code_phase - 150.0) <= 1.5
+    assert not O.is_detected(r2)
+
+
+def test_one_step_and_two_step_paths_agree():
+    # test/acquire.jl:158-195: one segment at N_nc = 1 and two at N_nc = 2 give the same decisions
+    # (48 dB-Hz instead of the reference's 45: over 1 ms, 45 dB-Hz is detected in 3 of 5 seeds of
+    # this noise generator, 48 dB-Hz in all of them)
+    fs, cp, dop = 2.048e6, 100.0, 1500.0
+    sig = _test_signal(G.GPSL1CA, 1, 2 * 2048, fs, dop, cp, 48, 123).astype(np.complex64)
+    p1 = O.plan_acquire(G.GPSL1CA, fs, [1])
+    p2 = O.plan_acquire(G.GPSL1CA, fs, [1], num_noncoherent_accumulations=2)
+    for plan, x in ((p1, sig[:2048]), (p2, sig)):
+        r = O.acquire_b(plan, x, [1])[0]
+        step = r.dopplers[1] - r.dopplers[0]
+        assert O.is_detected(r) and abs(r.code_phase - cp) < 1.0 and abs(r.carrier_doppler - dop) < step
+
+
+def test_sign_search_reports_the_doppler_without_a_half_band_offset():
+    # test/acquire.jl:197-230: with two data bits the reported Doppler lies within one bin of the truth
+    fs, cp, dop = 2.048e6, 100.0, 500.0
+    plan = O.plan_acquire(G.GPSL1CA, fs, [1], num_coherently_integrated_code_periods=40)
+    assert plan.num_data_bits == 2
+    r = O.acquire_b(plan, _test_signal(G.GPSL1CA, 1, 40 * 2048, fs, dop, cp, 45, 31).astype(np.complex64), [1])[0]
+    step = r.dopplers[1] - r.dopplers[0]
+    assert O.is_detected(r) and abs(r.code_phase - cp) <= 1.0 and abs(r.carrier_doppler - dop) < step
