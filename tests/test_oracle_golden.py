@@ -424,3 +424,46 @@ def test_sign_search_reports_the_doppler_without_a_half_band_offset():
     r = O.acquire_b(plan, _test_signal(G.GPSL1CA, 1, 40 * 2048, fs, dop, cp, 45, 31).astype(np.complex64), [1])[0]
     step = r.dopplers[1] - r.dopplers[0]
     assert O.is_detected(r) and abs(r.code_phase - cp) <= 1.0 and abs(r.carrier_doppler - dop) < step
+
+
+@pytest.mark.parametrize("cov,n_coh,dop,cp", [(10_000.0, 40, 0.0, 333.0), (20_000.0, 10, 1500.0, 100.0)])
+def test_doppler_grids_above_320_bins(cov, n_coh, dop, cp):
+    # test/acquire.jl:290-341: more than 320 Doppler bins (the reference's per-column FFT branches)
+    fs = 2.048e6
+    plan = O.plan_acquire(G.GPSL1CA, fs, [1], min_doppler_coverage=cov, num_coherently_integrated_code_periods=n_coh)
+    assert plan.num_doppler_bins > 320
+    r = O.acquire_b(plan, _test_signal(G.GPSL1CA, 1, n_coh * 2048, fs, dop, cp, 45, 17).astype(np.complex64), [1])[0]
+    assert O.is_detected(r) and abs(r.code_phase - cp) < 1.0
+
+
+def test_global_mean_estimator_on_the_one_step_path():
+    # test/acquire.jl:355-386: same peak as the opposite-row estimator, a different noise power, and
+    # the global mean of the stored surface outside +-floor(fs/fc) columns of the peak
+    # (src/est_signal_noise_power.jl:150-170)
+    fs = 2.048e6
+    sig = _test_signal(G.GPSL1CA, 4, 2048, fs, 750.0, 512.0, 45, 21).astype(np.complex64)
+    pg = O.plan_acquire(G.GPSL1CA, fs, [4], noise_estimator="global_mean")
+    po = O.plan_acquire(G.GPSL1CA, fs, [4])
+    rg = O.acquire_b(pg, sig, [4])[0]
+    ro = O.acquire_b(po, sig, [4])[0]
+    assert O.is_detected(rg)
+    assert (rg.code_phase, rg.carrier_doppler) == (ro.code_phase, ro.carrier_doppler)
+    assert rg.noise_power != ro.noise_power
+    rs = O.acquire_b(pg, sig, [4], store_power_bins=True)[0]
+    P = rs.power_bins.astype(np.float64)
+    half = int(fs // G.GPSL1CA.code_freq)
+    keep = np.ones(P.shape[1], bool)
+    keep[max(0, rs.peak_code_bin - half):min(P.shape[1], rs.peak_code_bin + half + 1)] = False
+    assert rs.noise_power == pytest.approx(P[:, keep].sum() / (keep.sum() * P.shape[0]), rel=1e-6)
+
+
+def test_multistep_interpolation_and_stored_surface():
+    # test/acquire.jl:435-460: N_nc = 4 with interpolation and the stored surface, reproducible
+    fs, cp = 2.048e6, 700.4
+    plan = O.plan_acquire(G.GPSL1CA, fs, [1], num_noncoherent_accumulations=4)
+    sig = _test_signal(G.GPSL1CA, 1, 4 * 2048, fs, 500.0, cp, 42, 8).astype(np.complex64)
+    r = O.acquire_b(plan, sig, [1], subsample_interpolation=True, store_power_bins=True)[0]
+    assert O.is_detected(r) and abs(r.code_phase - cp) <= 1.0
+    assert r.power_bins.shape == (plan.num_doppler_bins, plan.samples_per_code_eff)
+    r2 = O.acquire_b(plan, sig, [1], subsample_interpolation=True, store_power_bins=True)[0]
+    assert np.array_equal(r2.power_bins, r.power_bins)
