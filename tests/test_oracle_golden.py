@@ -467,3 +467,14 @@ def test_multistep_interpolation_and_stored_surface():
     assert r.power_bins.shape == (plan.num_doppler_bins, plan.samples_per_code_eff)
     r2 = O.acquire_b(plan, sig, [1], subsample_interpolation=True, store_power_bins=True)[0]
     assert np.array_equal(r2.power_bins, r.power_bins)
+
+
+@pytest.mark.parametrize("M,n_coh,cn0", [(2, 4, 40), (4, 4, 38), (8, 1, 42)])
+def test_weak_signal_passes_the_noncoherent_threshold(M, n_coh, cn0):
+    # test/cfar.jl:91-115: with M > 1 accumulations a real signal still clears the CFAR threshold
+    fs = 2.048e6
+    plan = O.plan_acquire(G.GPSL1CA, fs, list(range(1, 33)), num_coherently_integrated_code_periods=n_coh,
+                          num_noncoherent_accumulations=M)
+    sig = _test_signal(G.GPSL1CA, 7, n_coh * 2048 * M, fs, 500.0, 100.0, cn0, 9999 + M).astype(np.complex64)
+    r = O.acquire_b(plan, sig, [7])[0]
+    assert O.is_detected(r, pfa=0.01) and abs(r.code_phase - 100.0) < 1.0
