@@ -478,3 +478,46 @@ def test_weak_signal_passes_the_noncoherent_threshold(M, n_coh, cn0):
     sig = _test_signal(G.GPSL1CA, 7, n_coh * 2048 * M, fs, 500.0, 100.0, cn0, 9999 + M).astype(np.complex64)
     r = O.acquire_b(plan, sig, [7])[0]
     assert O.is_detected(r, pfa=0.01) and abs(r.code_phase - 100.0) < 1.0
+
+
+def test_l5i_gain_recovery_over_the_opt_out():
+    # test/secondary_code_search.jl:133-175: the rotation search recovers more than 8x the peak power
+    # of the search without the secondary code (theory 25x; the opt-out picks its best misalignment)
+    fs = 10.24e6
+    primary = G.gen_code(10240, G.GPSL5I, 1, fs).astype(np.complex64)
+    sig = np.concatenate([np.float32(G.NH10[k]) * primary for k in range(10)])
+    peaks = []
+    for use in (True, False):
+        plan = O.plan_acquire(G.GPSL5I, fs, [1], min_doppler_coverage=5000.0, num_coherently_integrated_code_periods=10,
+                              use_secondary_code=use)
+        peaks.append(O.acquire_b(plan, sig, [1], store_power_bins=True)[0].power_bins.max())
+    assert peaks[0] / peaks[1] > 8
+
+
+@pytest.mark.parametrize("cp,dop,n_nc", [(1234.5, 1000.0, 1), (5115.0, 1000.0, 1), (1234.5, 5000.0, 4)])
+def test_l5i_rotation_search_code_phase_and_doppler(cp, dop, n_nc):
+    # test/secondary_code_search.jl:177-206,294-386: the rotation search reports the Doppler without a
+    # half-band offset, also at the worst-case code phase (5115 chips: the primary-code wrap in the
+    # middle of a block) and with the code drift of four accumulation steps
+    fs = 12e6
+    plan = O.plan_acquire(G.GPSL5I, fs, [1], num_coherently_integrated_code_periods=10, num_noncoherent_accumulations=n_nc)
+    assert plan.num_secondary_rotations == 10
+    sig = _test_signal(G.GPSL5I, 1, n_nc * 10 * 12000, fs, dop, cp, 45, 29).astype(np.complex64)
+    r = O.acquire_b(plan, sig, [1])[0]
+    assert O.is_detected(r)
+    assert abs(r.code_phase - cp) <= (1.5 if n_nc > 1 else 1.0)
+    assert abs(r.carrier_doppler - dop) < plan.doppler_step
+
+
+@pytest.mark.parametrize("r0", [0, 3, 7, 9])
+def test_secondary_code_phase_exact_across_code_phase_and_doppler(r0):
+    # test/secondary_code_search.jl:260-292: the despread estimate is exact at every code phase
+    # (including the 5115-chip worst case) and Doppler
+    fs = 12e6
+    plan = O.plan_acquire(G.GPSL5I, fs, [1], num_coherently_integrated_code_periods=10)
+    for cp in (0.0, 2000.0, 5115.0, 9000.0):
+        primary = G.gen_code(12000, G.GPSL5I, 1, fs, start_phase=cp).astype(np.complex64)
+        base = np.concatenate([np.float32(G.NH10[(k + r0) % 10]) * primary for k in range(10)])
+        for dop in (0.0, 1300.0):
+            sig = base if dop == 0.0 else (base * np.exp(2j * np.pi * dop / fs * np.arange(len(base)))).astype(np.complex64)
+            assert O.acquire_b(plan, sig, [1])[0].secondary_code_phase == r0, (cp, dop)
