@@ -55,14 +55,15 @@ def test_peak_to_noise_ratio_consistent_with_cn0():
     assert strong.peak_to_noise_ratio > weak.peak_to_noise_ratio and strong.CN0 > weak.CN0
 
 
-def test_data_bit_transition_at_zero_doppler_keeps_the_peak():
-    # test/noncoherent_integration.jl:602-650 (two data bits, +1 -1)
+@pytest.mark.parametrize("n_coh", [40, 60])
+def test_data_bit_transition_at_zero_doppler_keeps_the_peak(n_coh):
+    # test/noncoherent_integration.jl:602-701 (data bits +1 -1 and +1 -1 +1)
     fs = 2.048e6
-    clean = _sig(G.GPSL1CA, 1, 40 * 2048, fs, 0.0, 0.0, 60, 42)
+    clean = _sig(G.GPSL1CA, 1, n_coh * 2048, fs, 0.0, 0.0, 60, 42)
     flipped = clean.copy()
-    flipped[20 * 2048:] *= -1
+    flipped[20 * 2048:40 * 2048] *= -1
     plan = A.plan_acquire(A.GPSL1CA(), fs, [1], min_doppler_coverage=10_000,
-                          num_coherently_integrated_code_periods=40)
+                          num_coherently_integrated_code_periods=n_coh)
     ref = A.acquire_b(plan, clean, 1)
     got = A.acquire_b(plan, flipped, 1)
     assert float(got.peak_power) == pytest.approx(float(ref.peak_power), rel=0.1)
@@ -176,3 +177,26 @@ def test_secondary_code_phase_exact_across_code_phase_and_doppler():
                 x = base if dop == 0.0 else (base * np.exp(2j * np.pi * dop / fs * np.arange(len(base)))).astype(
                     np.complex64)
                 assert A.acquire_b(plan, x, 1).secondary_code_phase == r0, (cp, r0, dop)
+
+
+def test_cfar_detection_with_synthetic_signal():
+    # test/cfar.jl:31-52: the planted PRN clears the threshold, at most 3 of the 31 absent ones do
+    fs = 2.048e6
+    plan = A.plan_acquire(A.GPSL1CA(), fs, list(range(1, 33)))
+    res = A.acquire_b(plan, _sig(G.GPSL1CA, 1, 2048, fs, 1000.0, 200.0, 45, 1), list(range(1, 33)))
+    thr = A.cfar_threshold(0.01, A.get_num_cells(res[0]))
+    assert res[0].prn == 1 and res[0].peak_to_noise_ratio > thr
+    assert sum(r.peak_to_noise_ratio > thr for r in res[1:]) <= 3
+
+
+def test_l5i_rotation_multi_symbol_data_flip():
+    # test/secondary_code_search.jl:208-258: 20 ms = two NH10 periods with a data flip between them
+    fs, n, cp, fd = 12e6, 20, 1234.5, 1000.0
+    primary = G.gen_code(12000, G.GPSL5I, 1, fs, start_phase=cp).astype(np.complex64)
+    x = np.concatenate([np.float32(G.NH10[k % 10] * (1 if k < 10 else -1)) * primary for k in range(n)])
+    x = (x * np.exp(2j * np.pi * fd / fs * np.arange(len(x)))).astype(np.complex64)
+    plan = A.plan_acquire(A.GPSL5I(), fs, [1], num_coherently_integrated_code_periods=n)
+    assert plan.num_secondary_rotations == 10
+    r = A.acquire_b(plan, x, 1)
+    assert A.is_detected(r) and abs(r.code_phase - cp) < 1.0 and abs(r.carrier_doppler - fd) < _step(plan)
+    assert r.secondary_code_phase == 0 and r.sign_pattern == 1
