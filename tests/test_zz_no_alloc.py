@@ -72,6 +72,25 @@ def test_noalloc_matches_acquire_on_consecutive_calls():
         _check(_noalloc(r.power_bins, fs, fc, est), r, fs, est)
 
 
+@pytest.mark.parametrize("est", [L.ACQ_NOISE_OPPOSITE_ROW, L.ACQ_NOISE_GLOBAL_MEAN])
+def test_noalloc_reference_known_answers(est):
+    # test/est_signal_noise_power.jl:1-98: a 29 x 1023 unit surface (fs 4 MHz, fc 1 MHz) with a 15 dB
+    # peak in the middle and at both corners, and for the opposite-row estimator an inflated band
+    # in the peak's row that the opposite row does not see
+    cases = [(10, 488, False), (0, 0, False), (28, 1022, False)]
+    if est == L.ACQ_NOISE_OPPOSITE_ROW:
+        cases.append((10, 488, True))
+    for r, c, band in cases:
+        P = np.ones((29, 1023), np.float32)
+        if band:
+            P[r, :] = 5.0
+        P[r, c] += np.float32(10 ** 1.5)
+        st = _noalloc(P, 4e6, 1e6, est)
+        assert (st.peak_doppler_bin, st.peak_code_bin) == (r, c)
+        assert st.noise_power == pytest.approx(1.0, rel=1e-6)
+        assert st.signal_power == pytest.approx(float(P[r, c]) - 1.0, rel=1e-6)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     import torch
     dummy = torch.zeros(16, dtype=torch.float32, device="cuda")
