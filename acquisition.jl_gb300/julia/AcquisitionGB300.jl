@@ -11,6 +11,9 @@
 # This environment has no Julia; the binding follows the header field by field.
 module AcquisitionGB300
 
+export plan_acquire, acquire!, acquire, AcquisitionPlan, AcquisitionResults, is_detected, get_num_cells,
+       cfar_threshold, OppositeRowNoiseEstimator, GlobalMeanNoiseEstimator, AcquisitionBatch, run!
+
 using GNSSSignals
 using Unitful: Hz, ustrip
 import ChainRulesCore
@@ -90,11 +93,47 @@ struct GlobalMeanNoiseEstimator end
 estid(::OppositeRowNoiseEstimator) = Int32(0)
 estid(::GlobalMeanNoiseEstimator) = Int32(1)
 
+# acq_geometry: the derived fields of AcquisitionPlan (src/plan.jl:81-174)
+struct Geometry
+    samples_per_code::Int32
+    samples_per_code_eff::Int32
+    num_blocks::Int32
+    block_size::Int32
+    fft_size::Int32
+    num_coherently_integrated_code_periods::Int32
+    num_data_bits::Int32
+    bit_edge_search_steps::Int32
+    num_noncoherent_accumulations::Int32
+    num_doppler_bins::Int32
+    num_secondary_rotations::Int32
+    bit_period_codes::Int32
+    num_prns::Int32
+    path::Int32
+    doppler_first_hz::Float64
+    doppler_step_hz::Float64
+    code_length::Float64
+    code_freq_hz::Float64
+    center_freq_hz::Float64
+    cfar_threshold_pfa001::Float64
+end
+
 mutable struct AcquisitionPlan
     h::Ptr{Cvoid}
     system::Any
     sampling_freq::Float64
-    avail_prns::Vector{Int32}
+    avail_prns::Vector{Int}
+    geometry::Geometry
+    doppler_freqs::AbstractRange
+    # per plan PRN: the cached power surface that results with store_power_bins alias (allocated on
+    # first use, overwritten by the next acquire! that stores power bins: test/plan.jl:329-355)
+    result_buffers::Vector{Union{Nothing,Matrix{Float32}}}
+end
+
+# plan.num_blocks, plan.samples_per_code, plan.num_secondary_rotations, ... as in the reference
+function Base.getproperty(p::AcquisitionPlan, s::Symbol)
+    s in fieldnames(AcquisitionPlan) && return getfield(p, s)
+    v = getfield(getfield(p, :geometry), s)
+    v isa Int32 ? Int(v) : v
 end
 
 function plan_acquire(system, sampling_freq, prns; min_doppler_coverage = 7000Hz,
@@ -113,15 +152,19 @@ function plan_acquire(system, sampling_freq, prns; min_doppler_coverage = 7000Hz
     # Int8) to use the package's chips bit for bit.
     check(ccall((:acq_plan_create, lib), Cint, (Ref{PlanDesc}, Ptr{Int32}, Int32, Ptr{Int8}, Ref{Ptr{Cvoid}}),
                 d, p, length(p), C_NULL, h))
-    plan = AcquisitionPlan(h[], system, fs, p)
-    finalizer(pl -> ccall((:acq_plan_destroy, lib), Cint, (Ptr{Cvoid},), pl.h), plan)
+    g = Ref{Geometry}()
+    st = ccall((:acq_plan_get_geometry, lib), Cint, (Ptr{Cvoid}, Ref{Geometry}), h[], g)
+    st == 0 || (ccall((:acq_plan_destroy, lib), Cint, (Ptr{Cvoid},), h[]); check(st))
+    dop = range(g[].doppler_first_hz * Hz; step = g[].doppler_step_hz * Hz, length = Int(g[].num_doppler_bins))
+    plan = AcquisitionPlan(h[], system, fs, Int.(p), g[], dop, Union{Nothing,Matrix{Float32}}[nothing for _ in p])
+    finalizer(pl -> ccall((:acq_plan_destroy, lib), Cint, (Ptr{Cvoid},), getfield(pl, :h)), plan)
 end
 
-struct AcquisitionResults
-    system::Any
+struct AcquisitionResults{S,D<:AbstractRange}
+    system::S
     prn::Int
-    sampling_frequency::Float64
-    carrier_doppler::Float64
+    sampling_frequency::typeof(1.0Hz)
+    carrier_doppler::typeof(1.0Hz)
     code_phase::Float64
     secondary_code_phase::Union{Int,Nothing}
     CN0::Float64
@@ -129,30 +172,114 @@ struct AcquisitionResults
     peak_to_noise_ratio::Float32
     num_noncoherent_integrations::Int
     power_bins::Union{Matrix{Float32},Nothing}
+    dopplers::D
+    num_blocks::Int
+    block_size::Int
+    num_secondary_rotations::Int
 end
 
-function acquire!(plan::AcquisitionPlan, signal::AbstractVector{T}, prns; interm_freq = 0.0Hz,
-                  subsample_interpolation = false, store_power_bins = false) where {T}
+function acquire!(plan::AcquisitionPlan, signal::AbstractVector{T}, prns::AbstractVector{<:Integer};
+                  interm_freq = 0.0Hz, subsample_interpolation::Bool = false,
+                  store_power_bins::Bool = false) where {T}
     p = Int32.(collect(prns))
     res = Vector{CResult}(undef, length(p))
+    nd, nc = plan.num_doppler_bins, plan.samples_per_code_eff
+    # per PRN row-major [doppler_row][code_col] from the library (ignored unless stored)
+    bins = Vector{Float32}(undef, store_power_bins ? length(p) * nd * nc : 0)
     flags = UInt32(subsample_interpolation) | (UInt32(store_power_bins) << 1)
     check(ccall((:acq_acquire, lib), Cint,
                 (Ptr{Cvoid}, Ptr{T}, Int32, Int64, Ptr{Int32}, Int32, Float64, UInt32, Ptr{CResult}, Ptr{Float32}),
                 plan.h, signal, dtype(T), length(signal), p, length(p), Float64(ustrip(Hz, interm_freq)), flags,
-                res, C_NULL))
-    [AcquisitionResults(plan.system, r.prn, plan.sampling_freq, r.carrier_doppler_hz, r.code_phase,
-                        r.secondary_code_phase < 0 ? nothing : Int(r.secondary_code_phase), r.cn0_dbhz,
-                        r.noise_power, r.peak_to_noise_ratio, r.num_noncoherent_integrations, nothing) for r in res]
+                res, bins))
+    map(enumerate(res)) do (i, r)
+        pb = nothing
+        if store_power_bins
+            slot = findfirst(==(Int(r.prn)), plan.avail_prns)
+            buf = plan.result_buffers[slot]
+            buf === nothing && (buf = plan.result_buffers[slot] = Matrix{Float32}(undef, nd, nc))
+            permutedims!(buf, reshape(view(bins, (i - 1) * nd * nc + 1:i * nd * nc), nc, nd), (2, 1))
+            pb = buf
+        end
+        AcquisitionResults(plan.system, Int(r.prn), plan.sampling_freq * Hz, r.carrier_doppler_hz * Hz, r.code_phase,
+                           r.secondary_code_phase < 0 ? nothing : Int(r.secondary_code_phase), r.cn0_dbhz,
+                           r.noise_power, r.peak_to_noise_ratio, Int(r.num_noncoherent_integrations), pb,
+                           plan.doppler_freqs, plan.num_blocks, plan.block_size, plan.num_secondary_rotations)
+    end
 end
 
-acquire(system, signal, sampling_freq, prns; kw...) =
-    acquire!(plan_acquire(system, sampling_freq, prns), signal, prns; kw...)
+# single-PRN convenience methods (src/acquire.jl:788-797, :872-882)
+acquire!(plan::AcquisitionPlan, signal, prn::Integer; kw...) = only(acquire!(plan, signal, [prn]; kw...))
+
+function acquire(system, signal, sampling_freq, prns::AbstractVector{<:Integer}; interm_freq = 0.0Hz,
+                 subsample_interpolation::Bool = false, store_power_bins::Bool = false, plan_kw...)
+    acquire!(plan_acquire(system, sampling_freq, prns; plan_kw...), signal, prns; interm_freq,
+             subsample_interpolation, store_power_bins)
+end
+acquire(system, signal, sampling_freq, prn::Integer; kw...) = only(acquire(system, signal, sampling_freq, [prn]; kw...))
 
 function cfar_threshold(pfa, num_cells; num_noncoherent_integrations = 1)
     out = Ref{Float64}(0)
     check(ccall((:acq_cfar_threshold, lib), Cint, (Float64, Int64, Int32, Ref{Float64}), pfa, num_cells,
                 num_noncoherent_integrations, out))
     out[]
+end
+
+# src/Acquisition.jl:124-142 (the rotation expansion counts, issue #70)
+get_num_cells(r::AcquisitionResults) = length(r.dopplers) * r.num_blocks * r.block_size * r.num_secondary_rotations
+
+is_detected(r::AcquisitionResults; pfa = 0.01) =
+    r.peak_to_noise_ratio > cfar_threshold(pfa, get_num_cells(r); num_noncoherent_integrations = r.num_noncoherent_integrations)
+
+# ---- ragged batches: many recordings and plans, one CUDA-graph launch per run ----
+struct BatchItem                # acq_batch_item
+    plan::Ptr{Cvoid}
+    dtype::Int32
+    n_samples::Int64
+    prns::Ptr{Int32}
+    n_prns::Int32
+    interm_freq_hz::Float64
+    flags::UInt32
+end
+
+mutable struct AcquisitionBatch
+    h::Ptr{Cvoid}
+    plans::Vector{AcquisitionPlan}   # kept alive: the batch holds their handles
+    prns::Vector{Vector{Int32}}
+end
+
+"""
+    AcquisitionBatch(items) with items = [(plan, signal, prns), ...] (or with a fourth element,
+    the intermediate frequency): captures one CUDA graph over every item; `run!(batch, signals)`
+    returns one result vector per item. Signals keep their element type and length per item.
+"""
+function AcquisitionBatch(items)
+    plans = [it[1] for it in items]
+    prns = [Int32.(collect(it[3])) for it in items]
+    c = [BatchItem(it[1].h, dtype(eltype(it[2])), length(it[2]), pointer(prns[i]), length(prns[i]),
+                   Float64(ustrip(Hz, length(it) > 3 ? it[4] : 0.0Hz)), UInt32(0)) for (i, it) in enumerate(items)]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve prns check(ccall((:acq_batch_create, lib), Cint, (Ptr{BatchItem}, Int32, Ref{Ptr{Cvoid}}),
+                                  c, length(c), h))
+    b = AcquisitionBatch(h[], plans, prns)
+    finalizer(x -> ccall((:acq_batch_destroy, lib), Cint, (Ptr{Cvoid},), x.h), b)
+end
+
+function run!(b::AcquisitionBatch, signals)
+    res = Vector{CResult}(undef, sum(length, b.prns))
+    ptrs = [Ptr{Cvoid}(pointer(s)) for s in signals]
+    GC.@preserve signals check(ccall((:acq_batch_run, lib), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{CResult}),
+                                     b.h, ptrs, res))
+    out, k = Vector{Vector{AcquisitionResults}}(), 0
+    for (plan, p) in zip(b.plans, b.prns)
+        push!(out, [AcquisitionResults(plan.system, Int(r.prn), plan.sampling_freq * Hz, r.carrier_doppler_hz * Hz,
+                                       r.code_phase, r.secondary_code_phase < 0 ? nothing : Int(r.secondary_code_phase),
+                                       r.cn0_dbhz, r.noise_power, r.peak_to_noise_ratio,
+                                       Int(r.num_noncoherent_integrations), nothing, plan.doppler_freqs,
+                                       plan.num_blocks, plan.block_size, plan.num_secondary_rotations)
+                    for r in res[k + 1:k + length(p)]])
+        k += length(p)
+    end
+    out
 end
 
 # ---- plan options (ACQ_OPT_* of include/acqgb300.h: launch shapes, kernel form, precision) ----

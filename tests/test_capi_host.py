@@ -53,6 +53,69 @@ def test_julia_option_table_matches_the_header():
     assert got == opts, set(got.items()) ^ set(opts.items())
 
 
+_C_SIZE = {"int32_t": 4, "uint32_t": 4, "int64_t": 8, "double": 8, "float": 4}
+_JL_SIZE = {"Int32": 4, "UInt32": 4, "Int64": 8, "Float64": 8, "Float32": 4}
+
+
+def _c_structs(header):
+    out = {}
+    for body, name in re.findall(r"typedef struct \{(.*?)\} (\w+);", header, re.S):
+        fields = []
+        for line in re.sub(r"/\*.*?\*/", "", body, flags=re.S).split(";"):
+            line = line.strip()
+            if not line:
+                continue
+            m = re.match(r"(?:const\s+)?(\w+)\s*(\*?)\s*(.*)", line)
+            typ, ptr, names = m.groups()
+            for nm in names.split(","):
+                nm = nm.strip().lstrip("*")
+                arr = re.match(r"(\w+)\[(\d+)\]", nm)
+                if arr:
+                    fields.append((arr.group(1), _C_SIZE[typ] * int(arr.group(2))))
+                else:
+                    fields.append((nm, 8 if ptr or "*" in names else _C_SIZE[typ]))
+        out[name] = fields
+    return out
+
+
+def _jl_struct(src, name):
+    """(field, bytes) of a plain-bits Julia struct of the binding."""
+    body = re.search(r"^struct %s\b[^\n]*\n(.*?)\nend" % name, src, re.S | re.M).group(1)
+    fields = []
+    for fname, typ in re.findall(r"^\s*(\w+)::(\S+)", body, re.M):
+        tup = re.match(r"NTuple\{(\d+),(\w+)\}", typ)
+        size = 8 if typ.startswith("Ptr{") else _JL_SIZE[tup.group(2)] * int(tup.group(1)) if tup else _JL_SIZE[typ]
+        fields.append((fname, size))
+    return fields
+
+
+def test_julia_binding_matches_the_header():
+    # the ccall module a maintainer of Acquisition.jl would add (not executed here: no Julia):
+    # its structs have the header's fields in the header's order and sizes, every symbol it
+    # calls is declared, and it binds the acquire path, the detection helpers and the batch API
+    header = open(os.path.join(ROOT, "include", "acqgb300.h")).read()
+    jl = open(os.path.join(ROOT, "acquisition.jl_gb300", "julia", "AcquisitionGB300.jl")).read()
+    c = _c_structs(header)
+    for jname, cname in [("PlanDesc", "acq_plan_desc"), ("Geometry", "acq_geometry"), ("CResult", "acq_result"),
+                         ("BatchItem", "acq_batch_item"), ("CorrCell", "acq_corr_cell"),
+                         ("CorrResult", "acq_corr_result")]:
+        assert _jl_struct(jl, jname) == c[cname], (jname, _jl_struct(jl, jname), c[cname])
+    declared = set(re.findall(r"\b(acq_\w+)\s*\(", header))
+    called = set(re.findall(r"ccall\(\(:(acq_\w+), lib\)", jl))
+    assert called <= declared, called - declared
+    assert {"acq_plan_create", "acq_plan_destroy", "acq_plan_get_geometry", "acq_acquire", "acq_cfar_threshold",
+            "acq_plan_set_option", "acq_plan_get_option", "acq_batch_create", "acq_batch_run", "acq_batch_destroy",
+            "acq_last_error"} <= called
+    for name in ("plan_acquire", "acquire!", "acquire", "is_detected", "get_num_cells", "cfar_threshold"):
+        assert re.search(r"^(function )?%s\(" % re.escape(name), jl, re.M), name
+    # the 15 fields of the reference's AcquisitionResults (src/Acquisition.jl:81-109), in order
+    res = re.search(r"^struct AcquisitionResults\{S,D<:AbstractRange\}\n(.*?)\nend", jl, re.S | re.M).group(1)
+    assert re.findall(r"^\s*(\w+)::", res, re.M) == [
+        "system", "prn", "sampling_frequency", "carrier_doppler", "code_phase", "secondary_code_phase", "CN0",
+        "noise_power", "peak_to_noise_ratio", "num_noncoherent_integrations", "power_bins", "dopplers", "num_blocks",
+        "block_size", "num_secondary_rotations"]
+
+
 def test_result_struct_layout():
     assert C.sizeof(L.Result) == 72
     assert C.sizeof(L.PlanDesc) == 56
