@@ -116,6 +116,19 @@ def test_julia_binding_matches_the_header():
         "block_size", "num_secondary_rotations"]
 
 
+def test_python_binding_structs_match_the_header():
+    # the ctypes structures the Python package passes through the C ABI: the header's fields, in
+    # order, with the header's sizes
+    from acqgb300 import batch as B
+    header = open(os.path.join(ROOT, "include", "acqgb300.h")).read()
+    c = _c_structs(header)
+    for cls, cname in [(L.PlanDesc, "acq_plan_desc"), (L.Geometry, "acq_geometry"), (L.Result, "acq_result"),
+                       (L.NoiseStats, "acq_noise_stats"), (L.SynthSat, "acq_synth_sat"), (L.CorrCell, "acq_corr_cell"),
+                       (L.CorrResult, "acq_corr_result"), (B.BatchItemC, "acq_batch_item")]:
+        got = [(name, C.sizeof(typ)) for name, typ in cls._fields_]
+        assert got == c[cname], (cname, got, c[cname])
+
+
 def test_result_struct_layout():
     assert C.sizeof(L.Result) == 72
     assert C.sizeof(L.PlanDesc) == 56
